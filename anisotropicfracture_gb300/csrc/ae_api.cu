@@ -1,0 +1,1074 @@
+// C ABI of libaefast.so (include/aefast.h): operator handle, multigrid hierarchy and
+// the MLMG-style solve driver.  Host C++; every field operation is a kernel launch on
+// the operator's stream.
+//
+// The cycle restates AMReX MLMG (tag 20.05, not part of the reference tree) as driven
+// by Solver::Nonlocal::Linear (src/Solver/Nonlocal/Linear.H:23-29,102-112):
+//   solve   : res0 = b - A x; target = max(tol_abs, tol_rel * max(|b|, |res0|)); repeat
+//             { cycle; x += cor; r = b - A x } until |r| <= target
+//   V-cycle : per level: cor = 0, nu1 smoother calls, rescor = res - A cor,
+//             res_{m+1} = R rescor; bottom solve; back up: cor += I cor_{m+1}, nu2 calls
+//   F-cycle : restrict res to every level, bottom solve, then for each level upwards:
+//             cor = I cor_{m+1}, res = res - A cor, V-cycle from that level, cor += saved
+//   bottom  : CG or BiCGStab to bottom_reltol, correction zeroed + nuf smoother calls on failure
+// Mixed precision: the cycle runs in FP32 (stiffness, diagonal, smoother, transfers)
+// inside an FP64 refinement loop whose residual, update, norms and bottom solve are FP64.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/aefast.h"
+#include "ae_launch.h"
+
+#define AE_CHECK(x)                                                                              \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) throw CudaErr(std::string(cudaGetErrorString(e_)) + " at " + \
+                                             __FILE__ + ":" + std::to_string(__LINE__), e_);     \
+    } while (0)
+
+namespace {
+
+using namespace ae;
+
+thread_local std::string g_last_error;
+
+struct ApiErr : std::runtime_error {
+    int code;
+    ApiErr(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+struct CudaErr : std::runtime_error {
+    cudaError_t err;
+    CudaErr(const std::string& m, cudaError_t e) : std::runtime_error(m), err(e) {}
+};
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return AE_OK;
+    } catch (const ApiErr& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const CudaErr& e) {
+        g_last_error = e.what();
+        return e.err == cudaErrorMemoryAllocation ? AE_ERR_OOM : AE_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return AE_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return (std::string(e.what()).find("out of memory") != std::string::npos) ? AE_ERR_OOM : AE_ERR_CUDA;
+    }
+}
+
+void require(bool ok, const std::string& msg, int code = AE_ERR_ARG) {
+    if (!ok) throw ApiErr(code, msg);
+}
+
+struct MGLevel {
+    Geo g;
+    long long nn = 0;
+    double *C = nullptr, *D = nullptr, *invD = nullptr;
+    double *res = nullptr, *cor = nullptr, *rescor = nullptr, *corhold = nullptr, *tmp = nullptr;
+    float *C32 = nullptr, *D32 = nullptr, *invD32 = nullptr;
+    float *res32 = nullptr, *cor32 = nullptr, *rescor32 = nullptr, *corhold32 = nullptr, *tmp32 = nullptr;
+};
+
+struct AmrLevel {
+    ae_level_desc desc;
+    std::vector<MGLevel> mg;
+    double *sol = nullptr, *rhs = nullptr;
+    bool model_set = false;
+};
+
+}  // namespace
+
+struct ae_op_s {
+    int model = 0, ncoef = 0;
+    BCP bc;
+    double bcval[26 * 3];
+    bool bc_set = false;
+    int uniform = 0, homogeneous = 0;
+    std::vector<AmrLevel> amr;
+    cudaStream_t st = nullptr;
+    cudaStream_t own_st = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    unsigned long long* dnorm = nullptr;  // device scratch: 8 norm slots
+    unsigned long long* hnorm = nullptr;  // pinned mirror
+    int* dflag = nullptr;                 // [0] NaN/zero-diagonal flags, [1] bottom failures
+    double* bottom_work = nullptr;
+    long long bottom_work_n = 0;
+    bool prepared = false;
+    bool have32 = false;
+    bool prepared32 = false;
+    long long bytes = 0;
+    std::vector<void*> allocs;
+    void* stage = nullptr;  // device staging for host fabs
+    size_t stage_bytes = 0;
+    void* stage2 = nullptr;
+    size_t stage2_bytes = 0;
+
+    template <class T>
+    T* alloc(long long n) {
+        void* p = nullptr;
+        AE_CHECK(cudaMalloc(&p, sizeof(T) * (size_t)(n > 0 ? n : 1)));
+        allocs.push_back(p);
+        bytes += sizeof(T) * n;
+        AE_CHECK(cudaMemsetAsync(p, 0, sizeof(T) * (size_t)(n > 0 ? n : 1), st));
+        return static_cast<T*>(p);
+    }
+    ~ae_op_s() {
+        for (void* p : allocs) cudaFree(p);
+        if (stage) cudaFree(stage);
+        if (stage2) cudaFree(stage2);
+        if (hnorm) cudaFreeHost(hnorm);
+        if (own_st) cudaStreamDestroy(own_st);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+    }
+    OpParams params(const Geo& g) const {
+        OpParams P;
+        P.g = g;
+        P.bc = bc;
+        P.model = model;
+        P.uniform = uniform;
+        return P;
+    }
+};
+
+namespace {
+
+int ncoef_of(int model) { return model == AE_MODEL_ISOTROPIC ? 2 : model == AE_MODEL_MAJORMINOR ? 21 : 9; }
+
+// Orders the operator's own stream after earlier work on the legacy default stream and the
+// legacy stream after the work an entry point enqueued, so that callers that produce and
+// consume device fields on the default stream (e.g. PyTorch) need no extra synchronisation.
+// A caller-provided stream (ae_op_set_stream) is left to the caller.
+struct StreamScope {
+    ae_op* op;
+    explicit StreamScope(ae_op* o) : op(o) {
+        if (op->st == op->own_st) {
+            AE_CHECK(cudaEventRecord(op->ev_in, cudaStreamLegacy));
+            AE_CHECK(cudaStreamWaitEvent(op->st, op->ev_in, 0));
+        }
+    }
+    ~StreamScope() {
+        if (op->st == op->own_st) {
+            cudaEventRecord(op->ev_out, op->st);
+            cudaStreamWaitEvent(cudaStreamLegacy, op->ev_out, 0);
+        }
+    }
+};
+
+// multigrid coarsening of AMR level 0: every cell count even, coarse count >= 2
+// (AMReX mg_domain_min_width = 2)
+bool coarsenable(const Geo& g) {
+    for (int d = 0; d < 3; ++d) {
+        const int nc = g.dhi[d] - g.dlo[d];
+        if (nc % 2 != 0 || nc / 2 < 2) return false;
+    }
+    return true;
+}
+
+Geo coarsen_geo(const Geo& g) {
+    Geo c = g;
+    for (int d = 0; d < 3; ++d) {
+        c.dlo[d] = g.dlo[d] / 2; c.dhi[d] = g.dhi[d] / 2;
+        c.vlo[d] = g.vlo[d] / 2; c.vhi[d] = g.vhi[d] / 2;
+        c.dx[d] = g.dx[d] * 2.0;
+    }
+    c.ng = 0;
+    return c;
+}
+
+template <class T>
+View<T> fab_view(const ae_fab& f) {
+    View<T> v;
+    v.p = static_cast<T*>(f.data);
+    for (int d = 0; d < 3; ++d) v.lo[d] = f.lo[d];
+    v.sy = f.hi[0] - f.lo[0] + 1;
+    v.sz = v.sy * (f.hi[1] - f.lo[1] + 1);
+    v.sc = v.sz * (f.hi[2] - f.lo[2] + 1);
+    return v;
+}
+Box3 fab_box(const ae_fab& f) {
+    Box3 b;
+    for (int d = 0; d < 3; ++d) { b.lo[d] = f.lo[d]; b.hi[d] = f.hi[d]; }
+    return b;
+}
+long long fab_elems(const ae_fab& f) { return box_npts(fab_box(f)) * f.ncomp; }
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void check_fab(const ae_fab* f, const Box3& need, int ncomp, const char* what) {
+    require(f != nullptr && f->data != nullptr, std::string(what) + ": null fab");
+    require(f->ncomp >= ncomp, std::string(what) + ": needs " + std::to_string(ncomp) + " components");
+    require(box_contains(fab_box(*f), need), std::string(what) + ": fab box does not cover the required region");
+}
+
+MGLevel& level_at(ae_op* op, int amrlev, int mglev) {
+    require(amrlev >= 0 && amrlev < (int)op->amr.size(), "amrlev out of range");
+    require(mglev >= 0 && mglev < (int)op->amr[amrlev].mg.size(), "mglev out of range");
+    return op->amr[amrlev].mg[mglev];
+}
+
+void ensure_stage(void*& buf, size_t& have, size_t need) {
+    if (have >= need) return;
+    if (buf) AE_CHECK(cudaFree(buf));
+    buf = nullptr;
+    AE_CHECK(cudaMalloc(&buf, need));
+    have = need;
+}
+
+// A device view of a fab of doubles: the fab itself if it is device memory, otherwise
+// an asynchronous copy into a staging buffer.
+View<const double> device_view_in(ae_op* op, const ae_fab& f, int slot) {
+    if (is_device_ptr(f.data)) return cview(fab_view<double>(f));
+    const size_t bytes = sizeof(double) * (size_t)fab_elems(f);
+    void*& buf = slot == 0 ? op->stage : op->stage2;
+    size_t& have = slot == 0 ? op->stage_bytes : op->stage2_bytes;
+    ensure_stage(buf, have, bytes);
+    AE_CHECK(cudaMemcpyAsync(buf, f.data, bytes, cudaMemcpyHostToDevice, op->st));
+    ae_fab d = f;
+    d.data = buf;
+    return cview(fab_view<double>(d));
+}
+
+void alloc_level_fp32(ae_op* op) {
+    if (op->have32) return;
+    for (auto& A : op->amr)
+        for (auto& L : A.mg) {
+            L.C32 = op->alloc<float>(op->ncoef * L.nn);
+            L.D32 = op->alloc<float>(3 * L.nn);
+            L.invD32 = op->alloc<float>(3 * L.nn);
+            L.res32 = op->alloc<float>(3 * L.nn);
+            L.cor32 = op->alloc<float>(3 * L.nn);
+            L.rescor32 = op->alloc<float>(3 * L.nn);
+            L.corhold32 = op->alloc<float>(3 * L.nn);
+            L.tmp32 = op->alloc<float>(3 * L.nn);
+        }
+    op->have32 = true;
+}
+
+// FP32 copies of the stiffness and diagonal on every level (mixed-precision cycle)
+void prepare32(ae_op* op) {
+    alloc_level_fp32(op);
+    if (op->prepared32) return;
+    for (auto& A : op->amr)
+        for (auto& L : A.mg) {
+            const Box3 s = geo_store(L.g);
+            launch_copy<float, double>(s, op->ncoef, level_view(L.g, L.C32), cview(level_view(L.g, L.C)), op->st);
+            launch_copy<float, double>(s, 3, level_view(L.g, L.D32), cview(level_view(L.g, L.D)), op->st);
+            launch_copy<float, double>(s, 3, level_view(L.g, L.invD32), cview(level_view(L.g, L.invD)), op->st);
+        }
+    AE_CHECK(cudaStreamSynchronize(op->st));
+    op->prepared32 = true;
+}
+
+double read_norm(ae_op* op, int slot) {
+    AE_CHECK(cudaMemcpyAsync(op->hnorm + slot, op->dnorm + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             op->st));
+    AE_CHECK(cudaStreamSynchronize(op->st));
+    double v;
+    std::memcpy(&v, op->hnorm + slot, sizeof(double));
+    return v;
+}
+
+// ------------------------------------------------------------------ prepare
+void prepare(ae_op* op) {
+    for (size_t a = 0; a < op->amr.size(); ++a)
+        require(op->amr[a].model_set, "SetModel has not been called on every AMR level", AE_ERR_STATE);
+    cudaStream_t st = op->st;
+    // Elastic<T>::averageDownCoeffs: restrict the stiffness down the MG levels of every AMR level
+    for (auto& A : op->amr)
+        for (size_t m = 1; m < A.mg.size(); ++m)
+            launch_restrict<double>(A.mg[m].g, op->ncoef, level_view(A.mg[m].g, A.mg[m].C),
+                                    cview(level_view(A.mg[m - 1].g, A.mg[m - 1].C)), st);
+    AE_CHECK(cudaMemsetAsync(op->dflag, 0, sizeof(int), st));
+    for (auto& A : op->amr)
+        for (auto& L : A.mg)
+            launch_diagonal<double>(op->params(L.g), cview(level_view(L.g, L.C)), level_view(L.g, L.D),
+                                    level_view(L.g, L.invD), op->dflag, st);
+    op->prepared32 = false;
+    int flag = 0;
+    AE_CHECK(cudaMemcpyAsync(&flag, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AE_CHECK(cudaStreamSynchronize(st));
+    op->prepared = true;
+    if (flag) {
+        op->prepared = false;
+        throw ApiErr(AE_ERR_NAN, "diagonal is NaN, infinite or zero on some node (Elastic<T>::Diagonal)");
+    }
+}
+
+// ------------------------------------------------------------------ the multigrid cycle
+template <class R>
+struct LevelPtrs {
+    R *C, *D, *invD, *res, *cor, *rescor, *corhold, *tmp;
+};
+template <class R>
+LevelPtrs<R> ptrs(MGLevel& L);
+template <>
+LevelPtrs<double> ptrs<double>(MGLevel& L) {
+    return {L.C, L.D, L.invD, L.res, L.cor, L.rescor, L.corhold, L.tmp};
+}
+template <>
+LevelPtrs<float> ptrs<float>(MGLevel& L) {
+    return {L.C32, L.D32, L.invD32, L.res32, L.cor32, L.rescor32, L.corhold32, L.tmp32};
+}
+
+template <class R>
+struct Cycle {
+    ae_op* op;
+    const ae_solver_opts& o;
+    std::vector<MGLevel>& lv;
+    cudaStream_t st;
+
+    // one smoother call (Fsmooth): o.sweeps Jacobi sweeps, x ping-pongs through tmp
+    void smooth(int m, R* x, const R* b) {
+        MGLevel& L = lv[m];
+        LevelPtrs<R> p = ptrs<R>(L);
+        const OpParams P = op->params(L.g);
+        R* a = x;
+        R* t = p.tmp;
+        for (int s = 0; s < o.sweeps; ++s) {
+            launch_jacobi<R>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.invD)),
+                             cview(level_view(L.g, p.D)), cview(level_view(L.g, a)), cview(level_view(L.g, b)),
+                             level_view(L.g, t), (R)o.omega, st);
+            std::swap(a, t);
+        }
+        if (a != x) launch_copy<R, R>(geo_store(L.g), 3, level_view(L.g, x), cview(level_view(L.g, a)), st);
+    }
+    // rescor = res - A cor
+    void res_of_cor(int m) {
+        MGLevel& L = lv[m];
+        LevelPtrs<R> p = ptrs<R>(L);
+        launch_residual<R>(op->params(L.g), cview(level_view(L.g, p.C)), cview(level_view(L.g, p.cor)),
+                           cview(level_view(L.g, p.res)), level_view(L.g, p.rescor), nullptr, nullptr, st);
+    }
+    void zero(int m, R* x) { launch_fill<R>(geo_store(lv[m].g), 3, level_view(lv[m].g, x), R(0), st); }
+    void restrict_res(int m, R* src) {  // res_{m+1} = R src_m
+        launch_restrict<R>(lv[m + 1].g, 3, level_view(lv[m + 1].g, ptrs<R>(lv[m + 1]).res),
+                           cview(level_view(lv[m].g, src)), st);
+    }
+    void interp_add(int m) {  // cor_m += I cor_{m+1}
+        launch_interp_add<R>(lv[m].g, 3, level_view(lv[m].g, ptrs<R>(lv[m]).cor),
+                             cview(level_view(lv[m + 1].g, ptrs<R>(lv[m + 1]).cor)), st);
+    }
+    void bottom() {
+        const int m = (int)lv.size() - 1;
+        MGLevel& L = lv[m];
+        const Box3 s = geo_store(L.g);
+        if (sizeof(R) == 4) launch_copy<double, R>(s, 3, level_view(L.g, L.res), cview(level_view(L.g, ptrs<R>(L).res)), st);
+        launch_fill<double>(s, 3, level_view(L.g, L.cor), 0.0, st);
+        BottomArgs a;
+        a.P = op->params(L.g);
+        a.K = make_scoef<double>(L.g);
+        a.C = L.C;
+        a.D = L.D;
+        a.invD = L.invD;
+        a.x = L.cor;
+        a.b = L.res;
+        a.work = op->bottom_work;
+        a.nn = L.nn;
+        a.bottom = o.bottom;
+        a.maxiter = o.bottom_max_iter;
+        a.reltol = o.bottom_reltol;
+        a.nuf = o.nuf;
+        a.sweeps = o.sweeps;
+        a.omega = o.omega;
+        a.fail_count = op->dflag + 1;
+        launch_bottom(a, st);
+        if (sizeof(R) == 4) launch_copy<R, double>(s, 3, level_view(L.g, ptrs<R>(L).cor), cview(level_view(L.g, L.cor)), st);
+    }
+    void vcycle(int top) {
+        const int bot = (int)lv.size() - 1;
+        for (int m = top; m < bot; ++m) {
+            LevelPtrs<R> p = ptrs<R>(lv[m]);
+            zero(m, p.cor);
+            for (int i = 0; i < o.nu1; ++i) smooth(m, p.cor, p.res);
+            res_of_cor(m);
+            restrict_res(m, p.rescor);
+        }
+        bottom();
+        for (int m = bot - 1; m >= top; --m) {
+            LevelPtrs<R> p = ptrs<R>(lv[m]);
+            interp_add(m);
+            for (int i = 0; i < o.nu2; ++i) smooth(m, p.cor, p.res);
+        }
+    }
+    void fcycle() {
+        const int bot = (int)lv.size() - 1;
+        for (int m = 0; m < bot; ++m) restrict_res(m, ptrs<R>(lv[m]).res);
+        bottom();
+        for (int m = bot - 1; m >= 0; --m) {
+            MGLevel& L = lv[m];
+            LevelPtrs<R> p = ptrs<R>(L);
+            const Box3 s = geo_store(L.g);
+            zero(m, p.cor);
+            interp_add(m);
+            res_of_cor(m);
+            launch_copy<R, R>(s, 3, level_view(L.g, p.res), cview(level_view(L.g, p.rescor)), st);
+            launch_copy<R, R>(s, 3, level_view(L.g, p.corhold), cview(level_view(L.g, p.cor)), st);
+            vcycle(m);
+            launch_axpy<R, R>(s, 3, level_view(L.g, p.cor), 1.0, cview(level_view(L.g, p.corhold)), st);
+        }
+    }
+    void run(bool f) {
+        if (f) fcycle();
+        else vcycle(0);
+    }
+};
+
+// One refinement step of a single-level solve on the stream: cycle, update, residual + norm.
+// Everything here is stream-ordered so it can be captured in a CUDA graph.
+void iteration_body(ae_op* op, const ae_solver_opts& o, bool fcyc) {
+    AmrLevel& A = op->amr[0];
+    MGLevel& L = A.mg[0];
+    cudaStream_t st = op->st;
+    const OpParams P = op->params(L.g);
+    const Box3 s = geo_store(L.g);
+    if (o.precision == 0) {
+        Cycle<double> cy{op, o, A.mg, st};
+        cy.run(fcyc);
+        launch_axpy<double, double>(s, 3, level_view(L.g, A.sol), 1.0, cview(level_view(L.g, L.cor)), st);
+        AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), st));
+        launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
+                                cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm, nullptr, st);
+    } else {
+        Cycle<float> cy{op, o, A.mg, st};
+        const int inner = o.inner_cycles > 0 ? o.inner_cycles : 1;
+        for (int c = 0; c < inner; ++c) {
+            cy.run(fcyc);
+            launch_axpy<double, float>(s, 3, level_view(L.g, A.sol), 1.0, cview(level_view(L.g, L.cor32)), st);
+            if (c + 1 < inner)  // FP32 residual of the correction equation, in place
+                launch_residual<float>(P, cview(level_view(L.g, L.C32)), cview(level_view(L.g, L.cor32)),
+                                       cview(level_view(L.g, L.res32)), level_view(L.g, L.res32), nullptr, nullptr,
+                                       st);
+        }
+        AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), st));
+        View<float> r32 = level_view(L.g, L.res32);
+        launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
+                                cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm, &r32, st);
+    }
+}
+
+void solve_single(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs, ae_solve_stats* stats) {
+    AmrLevel& A = op->amr[0];
+    MGLevel& L = A.mg[0];
+    cudaStream_t st = op->st;
+    const OpParams P = op->params(L.g);
+    const Box3 vreg = box_isect(geo_valid(L.g), geo_domain(L.g));
+    AE_CHECK(cudaMemsetAsync(op->dnorm, 0, 2 * sizeof(unsigned long long), st));
+    AE_CHECK(cudaMemsetAsync(op->dflag + 1, 0, sizeof(int), st));
+    launch_norminf<double>(vreg, 3, cview(level_view(L.g, A.rhs)), op->dnorm + 1, st);
+    View<float> r32 = o.precision ? level_view(L.g, L.res32) : View<float>{};
+    launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
+                            cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm,
+                            o.precision ? &r32 : nullptr, st);
+    const double res0 = read_norm(op, 0);
+    const double bnorm = read_norm(op, 1);
+    require(std::isfinite(res0) && std::isfinite(bnorm), "initial residual is NaN or infinite", AE_ERR_NAN);
+    const double max_norm = bnorm >= res0 ? bnorm : res0;
+    const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
+    double rn = res0;
+    int iters = 0, conv = res0 <= target;
+    // one CUDA graph per cycle kind (F, V), captured on first use
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    long long kernels_per_graph[2] = {0, 0};
+    auto cleanup = [&] {
+        for (int q = 0; q < 2; ++q) {
+            if (exec[q]) cudaGraphExecDestroy(exec[q]);
+            if (graph[q]) cudaGraphDestroy(graph[q]);
+        }
+    };
+    try {
+        while (!conv && iters < o.max_iter) {
+            const bool fcyc = iters < o.max_fmg_iter;
+            const int q = fcyc ? 0 : 1;
+            if (o.use_graph && !exec[q]) {
+                const long long c0 = g_kernel_launches.load();
+                AE_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                try {
+                    iteration_body(op, o, fcyc);
+                } catch (...) {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(st, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                AE_CHECK(cudaStreamEndCapture(st, &graph[q]));
+                AE_CHECK(cudaGraphInstantiate(&exec[q], graph[q], 0));
+                // captured launches execute only when the graph is replayed
+                kernels_per_graph[q] = g_kernel_launches.load() - c0;
+                g_kernel_launches.fetch_sub(kernels_per_graph[q]);
+            }
+            if (exec[q]) {
+                AE_CHECK(cudaGraphLaunch(exec[q], st));
+                g_kernel_launches.fetch_add(kernels_per_graph[q]);
+            } else {
+                iteration_body(op, o, fcyc);
+            }
+            rn = read_norm(op, 0);
+            ++iters;
+            if (o.verbose) fprintf(stderr, "aefast: iter %d |r|_inf = %.6e (target %.3e)\n", iters, rn, target);
+            require(std::isfinite(rn), "residual became NaN or infinite", AE_ERR_NAN);
+            if (rn <= target) conv = 1;
+        }
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
+    int fails = 0;
+    AE_CHECK(cudaMemcpyAsync(&fails, op->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AE_CHECK(cudaStreamSynchronize(st));
+    if (stats) {
+        stats->iters = iters;
+        stats->cycles = iters * (o.precision ? std::max(1, o.inner_cycles) : 1);
+        stats->converged = conv;
+        stats->nlevels = (int)A.mg.size();
+        stats->bottom_fail = fails;
+        stats->res0 = res0;
+        stats->resfinal = rn;
+        stats->target = target;
+    }
+    if (!conv) throw ApiErr(AE_ERR_NOT_CONVERGED, "MLMG failed to converge within max_iter");
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char* ae_last_error(void) { return g_last_error.c_str(); }
+const char* ae_version(void) { return "aefast 0.1 (sm_103a)"; }
+
+void ae_default_solver_opts(ae_solver_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->max_fmg_iter = 0;
+    o->nu1 = 1;
+    o->nu2 = 1;
+    o->sweeps = 2;
+    o->bottom = 0;
+    o->max_iter = 200;
+    o->bottom_max_iter = 200;
+    o->bottom_reltol = 1.0e-4;
+    o->nuf = 8;
+    o->max_mg_levels = 0;
+    o->omega = 2.0 / 3.0;
+    o->precision = 0;
+    o->inner_cycles = 1;
+    o->verbose = 0;
+    o->use_graph = 1;
+}
+
+int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) {
+    return guarded([&] {
+        require(out != nullptr, "out is null");
+        *out = nullptr;
+        require(levels != nullptr && nlev >= 1, "need at least one level");
+        require(model >= 0 && model <= 2, "unknown model kind");
+        std::unique_ptr<ae_op> op(new ae_op());
+        op->model = model;
+        op->ncoef = ncoef_of(model);
+        for (int f = 0; f < 26; ++f)
+            for (int d = 0; d < 3; ++d) { op->bc.t[f][d] = DISP; op->bcval[3 * f + d] = 0.0; }
+        op->amr.resize(nlev);
+        for (int a = 0; a < nlev; ++a) {
+            const ae_level_desc& L = levels[a];
+            AmrLevel& A = op->amr[a];
+            A.desc = L;
+            Geo g;
+            for (int d = 0; d < 3; ++d) {
+                require(L.domain_cells[d] >= 1, "domain needs at least one cell per direction");
+                require(L.dx[d] > 0.0, "dx must be positive");
+                require(L.lo[d] >= 0 && L.hi[d] <= L.domain_cells[d] && L.lo[d] < L.hi[d], "patch outside domain");
+                g.dlo[d] = 0;
+                g.dhi[d] = L.domain_cells[d];
+                g.vlo[d] = L.lo[d];
+                g.vhi[d] = L.hi[d];
+                g.dx[d] = L.dx[d];
+                if (a > 0) {
+                    const ae_level_desc& Pc = levels[a - 1];
+                    require(L.domain_cells[d] == 2 * Pc.domain_cells[d], "AMR levels must refine by 2");
+                    require(L.lo[d] % 2 == 0 && L.hi[d] % 2 == 0, "fine patch must align with coarse nodes");
+                    require(L.lo[d] / 2 >= Pc.lo[d] && L.hi[d] / 2 <= Pc.hi[d], "fine patch must nest in the coarse patch");
+                }
+            }
+            if (a == 0) {
+                for (int d = 0; d < 3; ++d)
+                    require(L.lo[d] == 0 && L.hi[d] == L.domain_cells[d], "AMR level 0 must cover its whole domain");
+                g.ng = 0;
+            } else {
+                g.ng = 2;
+            }
+            A.mg.push_back(MGLevel());
+            A.mg.back().g = g;
+            if (a == 0)
+                while (coarsenable(A.mg.back().g)) {
+                    MGLevel c;
+                    c.g = coarsen_geo(A.mg.back().g);
+                    A.mg.push_back(c);
+                }
+        }
+        // a non-blocking (capturable) stream; StreamScope orders it with the legacy stream
+        AE_CHECK(cudaStreamCreateWithFlags(&op->own_st, cudaStreamNonBlocking));
+        AE_CHECK(cudaEventCreateWithFlags(&op->ev_in, cudaEventDisableTiming));
+        AE_CHECK(cudaEventCreateWithFlags(&op->ev_out, cudaEventDisableTiming));
+        op->st = op->own_st;
+        AE_CHECK(cudaMallocHost(&op->hnorm, 8 * sizeof(unsigned long long)));
+        op->dnorm = op->alloc<unsigned long long>(8);
+        op->dflag = op->alloc<int>(4);
+        for (auto& A : op->amr) {
+            for (auto& L : A.mg) {
+                L.nn = box_npts(geo_store(L.g));
+                L.C = op->alloc<double>(op->ncoef * L.nn);
+                L.D = op->alloc<double>(3 * L.nn);
+                L.invD = op->alloc<double>(3 * L.nn);
+                L.res = op->alloc<double>(3 * L.nn);
+                L.cor = op->alloc<double>(3 * L.nn);
+                L.rescor = op->alloc<double>(3 * L.nn);
+                L.corhold = op->alloc<double>(3 * L.nn);
+                L.tmp = op->alloc<double>(3 * L.nn);
+            }
+            A.sol = op->alloc<double>(3 * A.mg[0].nn);
+            A.rhs = op->alloc<double>(3 * A.mg[0].nn);
+        }
+        const MGLevel& B = op->amr[0].mg.back();
+        op->bottom_work_n = 8 * 3 * B.nn;
+        op->bottom_work = op->alloc<double>(op->bottom_work_n);
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        *out = op.release();
+    });
+}
+
+int ae_op_destroy(ae_op* op) {
+    return guarded([&] {
+        if (!op) return;
+        cudaStreamSynchronize(op->st);
+        delete op;
+    });
+}
+
+int ae_op_set_stream(ae_op* op, void* stream) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        op->st = stream ? static_cast<cudaStream_t>(stream) : op->own_st;
+    });
+}
+
+int ae_op_set_model(ae_op* op, int amrlev, const ae_fab* coeffs) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        // Elastic<T>::SetModel copies the tilebox grown by the model's 2 ghosts ∩ domain
+        const Box3 need = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        check_fab(coeffs, need, op->ncoef, "SetModel");
+        require(!coeffs->is_float, "SetModel: coefficients must be double");
+        View<const double> src = device_view_in(op, *coeffs, 0);
+        launch_copy<double, double>(need, op->ncoef, level_view(L.g, L.C), src, op->st);
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        op->amr[amrlev].model_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_model_uniform(ae_op* op, const double* coeffs, int ncoef) {
+    return guarded([&] {
+        require(op != nullptr && coeffs != nullptr, "null argument");
+        require(ncoef == op->ncoef, "coefficient count does not match the model kind");
+        StreamScope scope_(op);
+        for (size_t a = 0; a < op->amr.size(); ++a) {
+            MGLevel& L = op->amr[a].mg[0];
+            std::vector<double> host((size_t)op->ncoef * L.nn);
+            for (int q = 0; q < op->ncoef; ++q)
+                for (long long n = 0; n < L.nn; ++n) host[(size_t)q * L.nn + n] = coeffs[q];
+            AE_CHECK(cudaMemcpyAsync(L.C, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, op->st));
+            AE_CHECK(cudaStreamSynchronize(op->st));
+            op->amr[a].model_set = true;
+        }
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_bc(ae_op* op, const int* type, const double* val) {
+    return guarded([&] {
+        require(op != nullptr && type != nullptr, "null argument");
+        for (int f = 0; f < 26; ++f)
+            for (int d = 0; d < 3; ++d) {
+                const int t = type[3 * f + d];
+                require(t >= 0 && t <= 3, "unknown BC type");
+                op->bc.t[f][d] = (unsigned char)t;
+                op->bcval[3 * f + d] = val ? val[3 * f + d] : 0.0;
+            }
+        op->bc_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_flags(ae_op* op, int uniform, int homogeneous) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        op->uniform = uniform ? 1 : 0;
+        op->homogeneous = homogeneous ? 1 : 0;
+    });
+}
+
+int ae_op_prepare(ae_op* op) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        prepare(op);
+    });
+}
+
+int ae_op_num_amr_levels(const ae_op* op) { return op ? (int)op->amr.size() : 0; }
+int ae_op_num_mg_levels(const ae_op* op, int amrlev) {
+    if (!op || amrlev < 0 || amrlev >= (int)op->amr.size()) return 0;
+    return (int)op->amr[amrlev].mg.size();
+}
+int ae_op_level_info(const ae_op* op, int amrlev, int mglev, int lo[3], int hi[3], int dom_hi[3], double dx[3]) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        const MGLevel& L = level_at(const_cast<ae_op*>(op), amrlev, mglev);
+        for (int d = 0; d < 3; ++d) {
+            if (lo) lo[d] = L.g.vlo[d];
+            if (hi) hi[d] = L.g.vhi[d];
+            if (dom_hi) dom_hi[d] = L.g.dhi[d];
+            if (dx) dx[d] = L.g.dx[d];
+        }
+    });
+}
+long long ae_op_device_bytes(const ae_op* op) { return op ? op->bytes : 0; }
+
+int ae_fapply(ae_op* op, int amrlev, int mglev, const ae_fab* out, const ae_fab* in) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, mglev);
+        require(op->amr[amrlev].model_set, "Fapply before SetModel", AE_ERR_STATE);
+        const Box3 reg = geo_apply_region(L.g);
+        const Box3 rd = box_isect(box_grow(reg, 1), geo_domain(L.g));
+        check_fab(in, rd, 3, "Fapply in");
+        check_fab(out, reg, 3, "Fapply out");
+        require(in->is_float == out->is_float, "Fapply: in and out must share a precision");
+        require(is_device_ptr(in->data) && is_device_ptr(out->data), "Fapply: fabs must be device memory");
+        const OpParams P = op->params(L.g);
+        if (in->is_float) {
+            require(op->prepared, "FP32 Fapply needs a prepared operator", AE_ERR_STATE);
+            prepare32(op);
+            launch_fapply<float>(P, cview(level_view(L.g, L.C32)), cview(fab_view<float>(*in)), fab_view<float>(*out),
+                                 op->st);
+        } else {
+            launch_fapply<double>(P, cview(level_view(L.g, L.C)), cview(fab_view<double>(*in)),
+                                  fab_view<double>(*out), op->st);
+        }
+    });
+}
+
+int ae_diagonal(ae_op* op, int amrlev, int mglev, const ae_fab* diag) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, mglev);
+        require(op->prepared, "Diagonal before prepare", AE_ERR_STATE);
+        const Box3 reg = geo_apply_region(L.g);
+        check_fab(diag, reg, 3, "Diagonal");
+        require(is_device_ptr(diag->data) && !diag->is_float, "Diagonal: device double fab required");
+        launch_copy<double, double>(reg, 3, fab_view<double>(*diag), cview(level_view(L.g, L.D)), op->st);
+    });
+}
+
+int ae_fsmooth(ae_op* op, int amrlev, int mglev, const ae_fab* x, const ae_fab* b, int nsweeps, double omega) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, mglev);
+        require(op->prepared, "Operator::Diagonal() must be called before using Fsmooth", AE_ERR_STATE);
+        require(nsweeps >= 0, "nsweeps must be non-negative");
+        const Box3 s = geo_store(L.g);
+        const Box3 need = box_isect(s, geo_domain(L.g));
+        check_fab(x, need, 3, "Fsmooth x");
+        check_fab(b, need, 3, "Fsmooth b");
+        require(x->is_float == b->is_float, "Fsmooth: x and b must share a precision");
+        require(is_device_ptr(x->data) && is_device_ptr(b->data), "Fsmooth: fabs must be device memory");
+        const OpParams P = op->params(L.g);
+        if (!x->is_float) {
+            // x -> internal ping-pong pair (tmp, rescor), sweeps, copy back
+            launch_copy<double, double>(need, 3, level_view(L.g, L.tmp), cview(fab_view<double>(*x)), op->st);
+            double *a = L.tmp, *t = L.rescor;
+            launch_copy<double, double>(s, 3, level_view(L.g, t), cview(level_view(L.g, a)), op->st);
+            for (int sw = 0; sw < nsweeps; ++sw) {
+                launch_jacobi<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, L.invD)),
+                                      cview(level_view(L.g, L.D)), cview(level_view(L.g, a)),
+                                      cview(fab_view<double>(*b)), level_view(L.g, t), omega, op->st);
+                std::swap(a, t);
+            }
+            launch_copy<double, double>(need, 3, fab_view<double>(*x), cview(level_view(L.g, a)), op->st);
+        } else {
+            prepare32(op);
+            launch_copy<float, float>(need, 3, level_view(L.g, L.tmp32), cview(fab_view<float>(*x)), op->st);
+            float *a = L.tmp32, *t = L.rescor32;
+            launch_copy<float, float>(s, 3, level_view(L.g, t), cview(level_view(L.g, a)), op->st);
+            for (int sw = 0; sw < nsweeps; ++sw) {
+                launch_jacobi<float>(P, cview(level_view(L.g, L.C32)), cview(level_view(L.g, L.invD32)),
+                                     cview(level_view(L.g, L.D32)), cview(level_view(L.g, a)),
+                                     cview(fab_view<float>(*b)), level_view(L.g, t), (float)omega, op->st);
+                std::swap(a, t);
+            }
+            launch_copy<float, float>(need, 3, fab_view<float>(*x), cview(level_view(L.g, a)), op->st);
+        }
+    });
+}
+
+int ae_residual(ae_op* op, int amrlev, int mglev, const ae_fab* r, const ae_fab* x, const ae_fab* b,
+                double* norm_inf) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, mglev);
+        const Box3 reg = geo_apply_region(L.g);
+        check_fab(x, box_isect(box_grow(reg, 1), geo_domain(L.g)), 3, "residual x");
+        check_fab(b, reg, 3, "residual b");
+        check_fab(r, reg, 3, "residual r");
+        require(!x->is_float && !b->is_float && !r->is_float, "residual: double fabs required");
+        require(is_device_ptr(x->data) && is_device_ptr(b->data) && is_device_ptr(r->data),
+                "residual: fabs must be device memory");
+        AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), op->st));
+        launch_residual<double>(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*x)),
+                                cview(fab_view<double>(*b)), fab_view<double>(*r), op->dnorm, nullptr, op->st);
+        const double n = read_norm(op, 0);
+        if (norm_inf) *norm_inf = n;
+    });
+}
+
+int ae_restrict(ae_op* op, int amrlev, int cmglev, const ae_fab* crse, const ae_fab* fine) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(cmglev >= 1, "cmglev must be >= 1");
+        StreamScope scope_(op);
+        MGLevel& Lc = level_at(op, amrlev, cmglev);
+        MGLevel& Lf = level_at(op, amrlev, cmglev - 1);
+        check_fab(crse, geo_valid(Lc.g), 3, "restriction crse");
+        check_fab(fine, box_isect(geo_valid(Lf.g), geo_domain(Lf.g)), 3, "restriction fine");
+        require(crse->is_float == fine->is_float, "restriction: precision mismatch");
+        require(is_device_ptr(crse->data) && is_device_ptr(fine->data), "restriction: fabs must be device memory");
+        if (crse->is_float)
+            launch_restrict<float>(Lc.g, 3, fab_view<float>(*crse), cview(fab_view<float>(*fine)), op->st);
+        else
+            launch_restrict<double>(Lc.g, 3, fab_view<double>(*crse), cview(fab_view<double>(*fine)), op->st);
+    });
+}
+
+int ae_interp_add(ae_op* op, int amrlev, int fmglev, const ae_fab* fine, const ae_fab* crse) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& Lf = level_at(op, amrlev, fmglev);
+        MGLevel& Lc = level_at(op, amrlev, fmglev + 1);
+        check_fab(fine, box_isect(geo_valid(Lf.g), geo_domain(Lf.g)), 3, "interpolation fine");
+        check_fab(crse, geo_valid(Lc.g), 3, "interpolation crse");
+        require(crse->is_float == fine->is_float, "interpolation: precision mismatch");
+        require(is_device_ptr(crse->data) && is_device_ptr(fine->data), "interpolation: fabs must be device memory");
+        if (fine->is_float)
+            launch_interp_add<float>(Lf.g, 3, fab_view<float>(*fine), cview(fab_view<float>(*crse)), op->st);
+        else
+            launch_interp_add<double>(Lf.g, 3, fab_view<double>(*fine), cview(fab_view<double>(*crse)), op->st);
+    });
+}
+
+int ae_bc_init(ae_op* op, int amrlev, const ae_fab* rhs, int homogeneous) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 need = box_isect(box_grow(geo_valid(L.g), L.g.ng < 2 ? L.g.ng : 2), geo_domain(L.g));
+        check_fab(rhs, need, 3, "BC Init rhs");
+        require(!rhs->is_float && is_device_ptr(rhs->data), "BC Init: device double fab required");
+        launch_bc_init(L.g, op->bc, op->bcval, homogeneous, fab_view<double>(*rhs), op->st);
+    });
+}
+
+int ae_strain(ae_op* op, int amrlev, const ae_fab* eps, const ae_fab* u, int voigt) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "Strain u");
+        check_fab(eps, v, voigt ? 6 : 9, "Strain eps");
+        require(is_device_ptr(u->data) && is_device_ptr(eps->data), "Strain: fabs must be device memory");
+        launch_strain(L.g, cview(fab_view<double>(*u)), fab_view<double>(*eps), voigt, op->st);
+    });
+}
+
+int ae_stress(ae_op* op, int amrlev, const ae_fab* sig, const ae_fab* u, int voigt) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "Stress u");
+        check_fab(sig, v, voigt ? 6 : 9, "Stress sigma");
+        require(is_device_ptr(u->data) && is_device_ptr(sig->data), "Stress: fabs must be device memory");
+        launch_stress(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
+                      fab_view<double>(*sig), voigt, op->st);
+    });
+}
+
+int ae_energy(ae_op* op, int amrlev, const ae_fab* w, const ae_fab* u) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "Energy u");
+        check_fab(w, v, 1, "Energy w");
+        require(is_device_ptr(u->data) && is_device_ptr(w->data), "Energy: fabs must be device memory");
+        launch_energy(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
+                      fab_view<double>(*w), op->st);
+    });
+}
+
+int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
+             const ae_solver_opts* opts, ae_solve_stats* stats) {
+    return guarded([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        require(op != nullptr && sol != nullptr && rhs != nullptr, "null argument");
+        StreamScope scope_(op);
+        ae_solver_opts o;
+        if (opts) o = *opts;
+        else ae_default_solver_opts(&o);
+        require(o.sweeps >= 1 && o.nu1 >= 0 && o.nu2 >= 0 && o.max_iter >= 0, "bad solver options");
+        require(o.bottom == 0 || o.bottom == 1, "bottom must be 0 (CG) or 1 (BiCGStab)");
+        require(op->amr.size() == 1, "multi-level AMR solve is not available in this build", AE_ERR_ARG);
+        if (!op->prepared) prepare(op);
+        if (o.precision) prepare32(op);
+        AmrLevel& A = op->amr[0];
+        MGLevel& L = A.mg[0];
+        const Box3 dom = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(&sol[0], dom, 3, "solve sol");
+        check_fab(&rhs[0], dom, 3, "solve rhs");
+        require(!sol[0].is_float && !rhs[0].is_float, "solve: double fabs required");
+        const bool sol_dev = is_device_ptr(sol[0].data);
+        View<const double> b = device_view_in(op, rhs[0], 0);
+        launch_copy<double, double>(dom, 3, level_view(L.g, A.rhs), b, op->st);
+        View<const double> x0 = device_view_in(op, sol[0], 1);
+        launch_copy<double, double>(dom, 3, level_view(L.g, A.sol), x0, op->st);
+        int status = AE_OK;
+        std::string msg;
+        try {
+            solve_single(op, o, tol_rel, tol_abs, stats);
+        } catch (const ApiErr& e) {
+            if (e.code != AE_ERR_NOT_CONVERGED) throw;
+            status = e.code;
+            msg = e.what();
+        }
+        // copy the solution out (also when not converged, as MLMG leaves its iterate in sol)
+        if (sol_dev) {
+            launch_copy<double, double>(dom, 3, fab_view<double>(sol[0]), cview(level_view(L.g, A.sol)), op->st);
+        } else {
+            const size_t bytes = sizeof(double) * (size_t)fab_elems(sol[0]);
+            ensure_stage(op->stage2, op->stage2_bytes, bytes);
+            ae_fab d = sol[0];
+            d.data = op->stage2;
+            launch_copy<double, double>(dom, 3, fab_view<double>(d), cview(level_view(L.g, A.sol)), op->st);
+            AE_CHECK(cudaMemcpyAsync(sol[0].data, op->stage2, bytes, cudaMemcpyDeviceToHost, op->st));
+        }
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (status != AE_OK) throw ApiErr(status, msg);
+    });
+}
+
+long long ae_kernel_launches(void) { return g_kernel_launches.load(); }
+
+int ae_profile_kernel(ae_op* op, int which, int amrlev, int mglev, int precision, int reps, double* avg_ms) {
+    return guarded([&] {
+        require(op != nullptr && avg_ms != nullptr && reps >= 1, "bad argument");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, mglev);
+        require(op->prepared, "profile needs a prepared operator", AE_ERR_STATE);
+        if (precision) prepare32(op);
+        require(which >= 0 && which <= 4, "which must be 0..4");
+        require(which < 3 || mglev + 1 < (int)op->amr[amrlev].mg.size(), "transfer needs a coarser level");
+        const OpParams P = op->params(L.g);
+        cudaStream_t st = op->st;
+        auto once = [&]() {
+            if (!precision) {
+                LevelPtrs<double> p = ptrs<double>(L);
+                if (which == 0)
+                    launch_fapply<double>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.cor)),
+                                          level_view(L.g, p.tmp), st);
+                else if (which == 1)
+                    launch_jacobi<double>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.invD)),
+                                          cview(level_view(L.g, p.D)), cview(level_view(L.g, p.cor)),
+                                          cview(level_view(L.g, p.res)), level_view(L.g, p.tmp), 2.0 / 3.0, st);
+                else if (which == 2)
+                    launch_residual<double>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.cor)),
+                                            cview(level_view(L.g, p.res)), level_view(L.g, p.rescor), nullptr,
+                                            nullptr, st);
+                else {
+                    MGLevel& Lc = op->amr[amrlev].mg[mglev + 1];
+                    if (which == 3)
+                        launch_restrict<double>(Lc.g, 3, level_view(Lc.g, Lc.rescor), cview(level_view(L.g, p.rescor)), st);
+                    else
+                        launch_interp_add<double>(L.g, 3, level_view(L.g, p.tmp), cview(level_view(Lc.g, Lc.cor)), st);
+                }
+            } else {
+                LevelPtrs<float> p = ptrs<float>(L);
+                if (which == 0)
+                    launch_fapply<float>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.cor)),
+                                         level_view(L.g, p.tmp), st);
+                else if (which == 1)
+                    launch_jacobi<float>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.invD)),
+                                         cview(level_view(L.g, p.D)), cview(level_view(L.g, p.cor)),
+                                         cview(level_view(L.g, p.res)), level_view(L.g, p.tmp), 2.0f / 3.0f, st);
+                else if (which == 2)
+                    launch_residual<float>(P, cview(level_view(L.g, p.C)), cview(level_view(L.g, p.cor)),
+                                           cview(level_view(L.g, p.res)), level_view(L.g, p.rescor), nullptr,
+                                           nullptr, st);
+                else {
+                    MGLevel& Lc = op->amr[amrlev].mg[mglev + 1];
+                    if (which == 3)
+                        launch_restrict<float>(Lc.g, 3, level_view(Lc.g, Lc.rescor32), cview(level_view(L.g, p.rescor)), st);
+                    else
+                        launch_interp_add<float>(L.g, 3, level_view(L.g, p.tmp), cview(level_view(Lc.g, Lc.cor32)), st);
+                }
+            }
+        };
+        once();  // warm-up
+        cudaEvent_t e0, e1;
+        AE_CHECK(cudaEventCreate(&e0));
+        AE_CHECK(cudaEventCreate(&e1));
+        AE_CHECK(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) once();
+        AE_CHECK(cudaEventRecord(e1, st));
+        AE_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        AE_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *avg_ms = (double)ms / reps;
+    });
+}
+
+}  // extern "C"

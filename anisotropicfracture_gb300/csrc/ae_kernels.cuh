@@ -1,0 +1,329 @@
+// Kernel templates of the nodal elastic operator.  Included by ae_kernels_f64.cu and
+// ae_kernels_f32.cu, each of which instantiates the launchers for one precision.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "ae_device.cuh"
+#include "ae_launch.h"
+
+namespace ae {
+
+#define AE_CUDA_CHECK(x)                                                                         \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess)                                                                   \
+            throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " \
+                                     + __FILE__ + ":" + std::to_string(__LINE__));               \
+    } while (0)
+
+constexpr int kBlock = 256;
+
+// Flattened iteration over a box: thread t -> (i, j, k), i fastest.
+struct Reg {
+    int lo[3];
+    unsigned nx, nxy;
+    unsigned n;
+};
+inline Reg make_reg(const Box3& b) {
+    Reg r;
+    for (int d = 0; d < 3; ++d) r.lo[d] = b.lo[d];
+    if (box_empty(b)) { r.nx = r.nxy = 1; r.n = 0; return r; }
+    r.nx = (unsigned)(b.hi[0] - b.lo[0] + 1);
+    r.nxy = r.nx * (unsigned)(b.hi[1] - b.lo[1] + 1);
+    r.n = r.nxy * (unsigned)(b.hi[2] - b.lo[2] + 1);
+    return r;
+}
+__device__ __forceinline__ void reg_ijk(const Reg& r, unsigned t, int& i, int& j, int& k) {
+    const unsigned kk = t / r.nxy;
+    const unsigned rem = t - kk * r.nxy;
+    const unsigned jj = rem / r.nx;
+    i = r.lo[0] + (int)(rem - jj * r.nx);
+    j = r.lo[1] + (int)jj;
+    k = r.lo[2] + (int)kk;
+}
+inline unsigned nblocks(unsigned n) { return (n + kBlock - 1) / kBlock; }
+
+// after every kernel launch: surface launch errors and count the launch
+inline void launched() {
+    AE_CUDA_CHECK(cudaGetLastError());
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+__device__ __forceinline__ bool in_box(const int lo[3], const int hi[3], int i, int j, int k) {
+    return i >= lo[0] && i <= hi[0] && j >= lo[1] && j <= hi[1] && k >= lo[2] && k <= hi[2];
+}
+
+// warp + block max of a non-negative double, then one atomicMax on its bit pattern
+__device__ __forceinline__ void block_max_atomic(double v, unsigned long long* out) {
+    __shared__ double sm[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? sm[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// ------------------------------------------------------------------ Fapply
+template <int M, class R>
+__global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg reg, View<const R> C, View<const R> u,
+                                                   View<R> f) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    R v[3];
+    apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, u.p, u.sc, u.at(i, j, k), u.sy,
+                     u.sz, i, j, k, v);
+    const long long o = f.at(i, j, k);
+    f.p[o] = v[0];
+    f.p[o + f.sc] = v[1];
+    f.p[o + 2 * f.sc] = v[2];
+}
+
+// ------------------------------------------------------------------ residual (+ norm, + FP32 copy)
+template <int M, class R, bool NORM, bool R32>
+__global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg reg, View<const R> C,
+                                                     View<const R> x, View<const R> b, View<R> r,
+                                                     unsigned long long* norm, View<float> r32) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    double mx = 0.0;
+    if (t < reg.n) {
+        int i, j, k;
+        reg_ijk(reg, t, i, j, k);
+        R v[3];
+        apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, x.p, x.sc, x.at(i, j, k),
+                         x.sy, x.sz, i, j, k, v);
+        const long long ob = b.at(i, j, k), orr = r.at(i, j, k);
+        const bool inv = in_box(P.g.vlo, P.g.vhi, i, j, k);
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const R rv = b.p[ob + n * b.sc] - v[n];
+            r.p[orr + n * r.sc] = rv;
+            if (R32) r32.p[r32.at(i, j, k) + n * r32.sc] = (float)rv;
+            if (NORM && inv) mx = fmax(mx, (double)fabs(rv));
+        }
+    }
+    if (NORM) block_max_atomic(mx, norm);
+}
+
+// ------------------------------------------------------------------ damped Jacobi sweep
+// src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in.
+template <int M, class R>
+__global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg reg, View<const R> C,
+                                                   View<const R> invD, View<const R> D, View<const R> xi,
+                                                   View<const R> b, View<R> xo, R omega) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const Geo& g = P.g;
+    const long long ox = xi.at(i, j, k), oo = xo.at(i, j, k);
+    // outside the domain: untouched
+    if (!in_box(g.dlo, g.dhi, i, j, k)) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) xo.p[oo + n * xo.sc] = xi.p[ox + n * xi.sc];
+        return;
+    }
+    // outermost ring of grow(valid, 2): zero
+    if (g.ng >= 2 && (i == g.vlo[0] - 2 || i == g.vhi[0] + 2 || j == g.vlo[1] - 2 || j == g.vhi[1] + 2 ||
+                      k == g.vlo[2] - 2 || k == g.vhi[2] + 2)) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) xo.p[oo + n * xo.sc] = R(0);
+        return;
+    }
+    R v[3];
+    apply_node<M, R>(g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, xi.p, xi.sc, ox, xi.sy, xi.sz, i,
+                     j, k, v);
+    const long long od = invD.at(i, j, k), ob = b.at(i, j, k);
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        const R xv = xi.p[ox + n * xi.sc];
+        const R dx = xv * D.p[od + n * D.sc];
+        const R rx = v[n] - dx;
+        xo.p[oo + n * xo.sc] = (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
+    }
+}
+
+// ------------------------------------------------------------------ Diagonal
+// src/Operator/Elastic.cpp:285-350: the operator applied to a unit spike, component by component.
+template <int M, class R>
+__global__ void __launch_bounds__(kBlock) k_diagonal(OpParams P, SCoef<R> K, Reg reg, View<const R> C, View<R> D,
+                                                     View<R> invD, int* nan_flag) {
+    constexpr int NC = NCoef<M>::value;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const Geo& g = P.g;
+    const long long cc = C.at(i, j, k), od = D.at(i, j, k);
+    const int ci[3] = {i, j, k};
+    bool mn[3], mx[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { mn[d] = ci[d] == g.dlo[d]; mx[d] = ci[d] == g.dhi[d]; }
+    R a[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) a[q] = C.p[cc + q * C.sc];
+    R nrm[3];
+    const int face = classify<R>(g, i, j, k, nrm);
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        R gu[3][3], bb[3][3][3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const R hi = (mx[d] && p == q) ? R(1) : R(0);
+                const R lo = (mn[d] && p == q) ? R(1) : R(0);
+                gu[q][d] = (hi - lo) / ((mn[d] || mx[d] ? R(1) : R(2)) * (R)g.dx[d]);
+            }
+#pragma unroll
+            for (int l = 0; l < 3; ++l)
+#pragma unroll
+                for (int jj = 0; jj < 3; ++jj) bb[q][l][jj] = R(0);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) bb[q][d][d] = (p == q) ? K.bb[d] : R(0);
+        }
+        R val;
+        if (face >= 0) {
+            const unsigned char tp = P.bc.t[face][p];
+            if (tp == DISP) val = R(1);
+            else if (tp == TRAC) {
+                R s[3][3];
+                stress_of<M, R>(a, gu, s);
+                val = s[p][0] * nrm[0] + s[p][1] * nrm[1] + s[p][2] * nrm[2];
+            } else if (tp == NEUMANN) val = gu[p][0] * nrm[0] + gu[p][1] * nrm[1] + gu[p][2] * nrm[2];
+            else val = R(0);
+        } else {
+            R f[3];
+            div_of<M, R>(a, bb, f);
+            val = f[p];  // the grad C term multiplies grad u = 0 at interior nodes
+        }
+        D.p[od + p * D.sc] = val;
+        invD.p[invD.at(i, j, k) + p * invD.sc] = R(1) / val;
+        if (!(fabs((double)val) <= 1.0e300) || val == R(0)) atomicExch(nan_flag, 1);
+    }
+}
+
+// ------------------------------------------------------------------ restriction / interpolation
+// src/Operator/Operator.cpp:486-543 (coarse node I, fine node 2I)
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_restrict(Geo gc, Reg reg, int ncomp, View<R> crse, View<const R> fine) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int I, J, Kc;
+    reg_ijk(reg, t, I, J, Kc);
+    const bool xe = I == gc.dlo[0] || I == gc.dhi[0];
+    const bool ye = J == gc.dlo[1] || J == gc.dhi[1];
+    const bool ze = Kc == gc.dlo[2] || Kc == gc.dhi[2];
+    const long long sy = fine.sy, sz = fine.sz;
+    for (int n = 0; n < ncomp; ++n) {
+        const R* f = fine.p + fine.at(2 * I, 2 * J, 2 * Kc) + n * fine.sc;
+        R v;
+        if (xe && ye && ze) v = f[0];
+        else if (ye && ze) v = R(0.25) * f[-1] + R(0.5) * f[0] + R(0.25) * f[1];
+        else if (ze && xe) v = R(0.25) * f[-sy] + R(0.5) * f[0] + R(0.25) * f[sy];
+        else if (xe && ye) v = R(0.25) * f[-sz] + R(0.5) * f[0] + R(0.25) * f[sz];
+        else if (xe)
+            v = (f[-sy - sz] + R(2) * f[-sz] + f[sy - sz] + R(2) * f[-sy] + R(4) * f[0] + R(2) * f[sy] + f[-sy + sz] +
+                 R(2) * f[sz] + f[sy + sz]) * R(1.0 / 16.0);
+        else if (ye)
+            v = (f[-1 - sz] + R(2) * f[-1] + f[-1 + sz] + R(2) * f[-sz] + R(4) * f[0] + R(2) * f[sz] + f[1 - sz] +
+                 R(2) * f[1] + f[1 + sz]) * R(1.0 / 16.0);
+        else if (ze)
+            v = (f[-1 - sy] + R(2) * f[-sy] + f[1 - sy] + R(2) * f[-1] + R(4) * f[0] + R(2) * f[1] + f[-1 + sy] +
+                 R(2) * f[sy] + f[1 + sy]) * R(1.0 / 16.0);
+        else
+            v = (f[-1 - sy - sz] + f[-1 - sy + sz] + f[-1 + sy - sz] + f[-1 + sy + sz] + f[1 - sy - sz] +
+                 f[1 - sy + sz] + f[1 + sy - sz] + f[1 + sy + sz]) * R(1.0 / 64.0) +
+                (f[-sy - sz] + f[-sy + sz] + f[sy - sz] + f[sy + sz] + f[-1 - sz] + f[1 - sz] + f[-1 + sz] +
+                 f[1 + sz] + f[-1 - sy] + f[-1 + sy] + f[1 - sy] + f[1 + sy]) * R(1.0 / 32.0) +
+                (f[-1] + f[-sy] + f[-sz] + f[1] + f[sy] + f[sz]) * R(1.0 / 16.0) + f[0] * R(1.0 / 8.0);
+        crse.p[crse.at(I, J, Kc) + n * crse.sc] = v;
+    }
+}
+
+// src/Operator/Operator.cpp:589-618 (fine node (i,j,k), coarse node (i/2, j/2, k/2))
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_interp_add(Reg reg, int ncomp, View<R> fine, View<const R> crse) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const int I = i >> 1, J = j >> 1, Kc = k >> 1;  // non-negative indices
+    const bool ie = !(i & 1), je = !(j & 1), ke = !(k & 1);
+    const long long sy = crse.sy, sz = crse.sz;
+    for (int n = 0; n < ncomp; ++n) {
+        const R* c = crse.p + crse.at(I, J, Kc) + n * crse.sc;
+        R v;
+        if (ie && je && ke) v = c[0];
+        else if (je && ke) v = R(0.5) * (c[0] + c[1]);
+        else if (ke && ie) v = R(0.5) * (c[0] + c[sy]);
+        else if (ie && je) v = R(0.5) * (c[0] + c[sz]);
+        else if (ie) v = R(0.25) * (c[0] + c[sy] + c[sz] + c[sy + sz]);
+        else if (je) v = R(0.25) * (c[0] + c[sz] + c[1] + c[1 + sz]);
+        else if (ke) v = R(0.25) * (c[0] + c[1] + c[sy] + c[1 + sy]);
+        else v = R(0.125) * (c[0] + c[1] + c[sy] + c[sz] + c[sy + sz] + c[1 + sz] + c[1 + sy] + c[1 + sy + sz]);
+        fine.p[fine.at(i, j, k) + n * fine.sc] += v;
+    }
+}
+
+// ------------------------------------------------------------------ elementwise
+template <class Ro, class Ri>
+__global__ void __launch_bounds__(kBlock) k_copy(Reg reg, int ncomp, View<Ro> dst, View<const Ri> src) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long od = dst.at(i, j, k), os = src.at(i, j, k);
+    for (int n = 0; n < ncomp; ++n) dst.p[od + n * dst.sc] = (Ro)src.p[os + n * src.sc];
+}
+template <class Ro, class Ri>
+__global__ void __launch_bounds__(kBlock) k_axpy(Reg reg, int ncomp, View<Ro> dst, double alpha, View<const Ri> src) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long od = dst.at(i, j, k), os = src.at(i, j, k);
+    for (int n = 0; n < ncomp; ++n) dst.p[od + n * dst.sc] += (Ro)(alpha * (double)src.p[os + n * src.sc]);
+}
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_fill(Reg reg, int ncomp, View<R> dst, R value) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long od = dst.at(i, j, k);
+    for (int n = 0; n < ncomp; ++n) dst.p[od + n * dst.sc] = value;
+}
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_norminf(Reg reg, int ncomp, View<const R> v, unsigned long long* out) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    double mx = 0.0;
+    if (t < reg.n) {
+        int i, j, k;
+        reg_ijk(reg, t, i, j, k);
+        const long long o = v.at(i, j, k);
+        for (int n = 0; n < ncomp; ++n) mx = fmax(mx, (double)fabs(v.p[o + n * v.sc]));
+    }
+    block_max_atomic(mx, out);
+}
+
+// ------------------------------------------------------------------ launcher bodies
+template <class R, class F>
+inline void dispatch_model(int model, F&& f) {
+    if (model == ISO) f(std::integral_constant<int, ISO>());
+    else if (model == MM) f(std::integral_constant<int, MM>());
+    else f(std::integral_constant<int, DIAG>());
+}
+
+}  // namespace ae

@@ -1,0 +1,341 @@
+// FP64 instantiation of the operator kernels, plus the FP64-only kernels: boundary
+// values, post-processing fields and the single-CTA bottom solver.
+#include <type_traits>
+
+#include "ae_kernels.cuh"
+
+#define AE_REAL double
+#include "ae_kernels_common.inc"
+#undef AE_REAL
+
+namespace ae {
+
+std::atomic<long long> g_kernel_launches{0};
+
+AE_INST_COPY(double, double)
+AE_INST_COPY(double, float)
+
+// ------------------------------------------------------------------ BC::Operator::Elastic::Init
+// src/BC/Operator/Elastic.H:106-181: boundary values into the rhs on every domain-boundary node.
+struct BCVal {
+    double v[26][3];
+};
+__global__ void __launch_bounds__(kBlock) k_bc_init(Geo g, BCP bc, BCVal val, int homogeneous, Reg reg,
+                                                    View<double> rhs) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double n[3];
+    const int face = classify<double>(g, i, j, k, n);
+    if (face < 0) return;
+    const long long o = rhs.at(i, j, k);
+    for (int dir = 0; dir < 3; ++dir)
+        rhs.p[o + dir * rhs.sc] = (homogeneous && bc.t[face][dir] == DISP) ? 0.0 : val.v[face][dir];
+}
+void launch_bc_init(const Geo& g, const BCP& bc, const double* val, int homogeneous, View<double> rhs,
+                    cudaStream_t st) {
+    const Box3 region = box_isect(box_grow(geo_valid(g), g.ng < 2 ? g.ng : 2), geo_domain(g));
+    const Reg reg = make_reg(region);
+    if (reg.n == 0) return;
+    BCVal v;
+    for (int f = 0; f < 26; ++f)
+        for (int d = 0; d < 3; ++d) v.v[f][d] = val[3 * f + d];
+    k_bc_init<<<nblocks(reg.n), kBlock, 0, st>>>(g, bc, v, homogeneous, reg, rhs);
+    launched();
+}
+
+// ------------------------------------------------------------------ Strain / Stress / Energy
+// src/Operator/Elastic.cpp:399-572 (valid box, boundary-aware first derivatives)
+__device__ __forceinline__ void grad_at(const Geo& g, const SCoef<double>& K, const View<const double>& u, int i,
+                                        int j, int k, double gu[3][3]) {
+    const int ci[3] = {i, j, k};
+    const long long os[3] = {1, u.sy, u.sz};
+    const long long o = u.at(i, j, k);
+    for (int p = 0; p < 3; ++p) {
+        const double* up = u.p + o + p * u.sc;
+        for (int d = 0; d < 3; ++d) {
+            const long long s = os[d];
+            if (ci[d] == g.dlo[d]) gu[p][d] = (up[s] - up[0]) * K.id[d];
+            else if (ci[d] == g.dhi[d]) gu[p][d] = (up[0] - up[-s]) * K.id[d];
+            else gu[p][d] = (up[s] - up[-s]) * K.h[d];
+        }
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_strain(Geo g, SCoef<double> K, Reg reg, View<const double> u,
+                                                   View<double> e, int voigt) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3];
+    grad_at(g, K, u, i, j, k, gu);
+    double s[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) s[a][b] = 0.5 * (gu[a][b] + gu[b][a]);
+    const long long o = e.at(i, j, k);
+    if (voigt) {
+        const double v[6] = {s[0][0], s[1][1], s[2][2], s[1][2], s[2][0], s[0][1]};
+        for (int q = 0; q < 6; ++q) e.p[o + q * e.sc] = v[q];
+    } else {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) e.p[o + (3 * a + b) * e.sc] = s[a][b];
+    }
+}
+template <int M>
+__global__ void __launch_bounds__(kBlock) k_stress(Geo g, SCoef<double> K, Reg reg, View<const double> C,
+                                                   View<const double> u, View<double> sg, int voigt, int energy) {
+    constexpr int NC = NCoef<M>::value;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3], s[3][3], a[NC];
+    grad_at(g, K, u, i, j, k, gu);
+    const long long cc = C.at(i, j, k);
+    for (int q = 0; q < NC; ++q) a[q] = C.p[cc + q * C.sc];
+    stress_of<M, double>(a, gu, s);
+    const long long o = sg.at(i, j, k);
+    if (energy) {
+        // W(gradu) = trace(0.5 gradu^T (C gradu)), then += sum 0.5 sig:eps (Elastic.cpp:557-569)
+        double w = 0.0;
+        for (int ii = 0; ii < 3; ++ii) {
+            double tt = 0.0;
+            for (int jj = 0; jj < 3; ++jj) tt += gu[jj][ii] * s[jj][ii];
+            w += 0.5 * tt;
+        }
+        for (int m = 0; m < 3; ++m)
+            for (int n = 0; n < 3; ++n) w += .5 * s[m][n] * (.5 * (gu[m][n] + gu[n][m]));
+        sg.p[o] = w;
+    } else if (voigt) {
+        const double v[6] = {s[0][0], s[1][1], s[2][2], s[1][2], s[2][0], s[0][1]};
+        for (int q = 0; q < 6; ++q) sg.p[o + q * sg.sc] = v[q];
+    } else {
+        for (int a2 = 0; a2 < 3; ++a2)
+            for (int b = 0; b < 3; ++b) sg.p[o + (3 * a2 + b) * sg.sc] = s[a2][b];
+    }
+}
+void launch_strain(const Geo& g, View<const double> u, View<double> e, int voigt, cudaStream_t st) {
+    const Reg reg = make_reg(box_isect(geo_valid(g), geo_domain(g)));
+    if (reg.n == 0) return;
+    k_strain<<<nblocks(reg.n), kBlock, 0, st>>>(g, make_scoef<double>(g), reg, u, e, voigt);
+    launched();
+}
+void launch_stress(const OpParams& P, View<const double> C, View<const double> u, View<double> s, int voigt,
+                   cudaStream_t st) {
+    const Reg reg = make_reg(box_isect(geo_valid(P.g), geo_domain(P.g)));
+    if (reg.n == 0) return;
+    dispatch_model<double>(P.model, [&](auto m) {
+        k_stress<decltype(m)::value><<<nblocks(reg.n), kBlock, 0, st>>>(P.g, make_scoef<double>(P.g), reg, C, u, s,
+                                                                        voigt, 0);
+    });
+    launched();
+}
+void launch_energy(const OpParams& P, View<const double> C, View<const double> u, View<double> w, cudaStream_t st) {
+    const Reg reg = make_reg(box_isect(geo_valid(P.g), geo_domain(P.g)));
+    if (reg.n == 0) return;
+    dispatch_model<double>(P.model, [&](auto m) {
+        k_stress<decltype(m)::value><<<nblocks(reg.n), kBlock, 0, st>>>(P.g, make_scoef<double>(P.g), reg, C, u, w,
+                                                                        0, 1);
+    });
+    launched();
+}
+
+// ------------------------------------------------------------------ bottom solve (one CTA)
+// MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab restated; the whole
+// Krylov loop runs inside one thread block on the coarsest level (ng = 0, storage = domain).
+constexpr int kBottomThreads = 256;
+
+struct BlkRed {
+    double part[kBottomThreads / 32];
+    double res[2];
+};
+__device__ __forceinline__ double blk_sum(double v, BlkRed& sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh.part[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh.part[q];
+        sh.res[0] = s;
+    }
+    __syncthreads();
+    const double r = sh.res[0];
+    __syncthreads();
+    return r;
+}
+__device__ __forceinline__ double blk_max(double v, BlkRed& sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh.part[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s = fmax(s, sh.part[q]);
+        sh.res[0] = s;
+    }
+    __syncthreads();
+    const double r = sh.res[0];
+    __syncthreads();
+    return r;
+}
+
+template <int M>
+struct BottomOps {
+    const BottomArgs& a;
+    SCoef<double> K;
+    View<const double> Cv;
+    long long sy, sz, nn;
+    int nx, ny, nz;
+    __device__ BottomOps(const BottomArgs& aa) : a(aa) {
+        K = aa.K;
+        const Geo& g = aa.P.g;
+        nx = g.vhi[0] - g.vlo[0] + 1;
+        ny = g.vhi[1] - g.vlo[1] + 1;
+        nz = g.vhi[2] - g.vlo[2] + 1;
+        sy = nx;
+        sz = (long long)nx * ny;
+        nn = sz * nz;
+        Cv.p = aa.C;
+        Cv.lo[0] = g.vlo[0]; Cv.lo[1] = g.vlo[1]; Cv.lo[2] = g.vlo[2];
+        Cv.sy = sy; Cv.sz = sz; Cv.sc = nn;
+    }
+    // out = A x over every node
+    __device__ void apply(const double* x, double* out) const {
+        const Geo& g = a.P.g;
+        for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+            const int k = (int)(t / sz), rem = (int)(t - (long long)k * sz);
+            const int j = rem / nx, i = rem - j * nx;
+            double v[3];
+            apply_node<M, double>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz, i + g.vlo[0],
+                                  j + g.vlo[1], k + g.vlo[2], v);
+            out[t] = v[0];
+            out[t + nn] = v[1];
+            out[t + 2 * nn] = v[2];
+        }
+        __syncthreads();
+    }
+    __device__ double dot(const double* x, const double* y, BlkRed& sh) const {
+        double s = 0.0;
+        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) s += x[t] * y[t];
+        return blk_sum(s, sh);
+    }
+    __device__ double ninf(const double* x, BlkRed& sh) const {
+        double s = 0.0;
+        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) s = fmax(s, fabs(x[t]));
+        return blk_max(s, sh);
+    }
+    // one Fsmooth call: a.sweeps damped-Jacobi sweeps (ng = 0: every node is updated)
+    __device__ void smooth(double* x, const double* b, double* tmp) const {
+        for (int s = 0; s < a.sweeps; ++s) {
+            apply(x, tmp);
+            for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
+                const double xv = x[t];
+                const double rx = tmp[t] - xv * a.D[t];
+                x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * a.invD[t];
+            }
+            __syncthreads();
+        }
+    }
+};
+
+template <int M>
+__global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
+    __shared__ BlkRed sh;
+    const BottomOps<M> ops(a);
+    const long long N = 3 * ops.nn;
+    double* x = a.x;
+    const double* b = a.b;
+    double* r = a.work;
+    double* p = r + N;
+    double* q = p + N;
+    double* rh = q + N;
+    double* v = rh + N;
+    double* tt = v + N;
+    double* sorig = tt + N;
+    double* tmp = sorig + N;
+    const double eps_rel = a.reltol, eps_abs = -1.0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) sorig[t] = x[t];
+    __syncthreads();
+    ops.apply(x, tmp);
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) { r[t] = b[t] - tmp[t]; x[t] = 0.0; }
+    __syncthreads();
+    double rnorm = ops.ninf(r, sh);
+    const double rnorm0 = rnorm;
+    int ret = 0;
+    if (!(rnorm0 == 0.0 || rnorm0 < eps_abs)) {
+        if (a.bottom == 0) {
+            double rho_1 = 0.0;
+            for (int iter = 1; iter <= a.maxiter; ++iter) {
+                const double rho = ops.dot(r, r, sh);  // z = r (no preconditioner)
+                if (rho == 0.0) { ret = 1; break; }
+                const double beta = iter == 1 ? 0.0 : rho / rho_1;
+                for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = iter == 1 ? r[t] : r[t] + beta * p[t];
+                __syncthreads();
+                ops.apply(p, q);
+                const double pw = ops.dot(p, q, sh);
+                if (pw == 0.0) { ret = 1; break; }
+                const double alpha = rho / pw;
+                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * q[t]; }
+                __syncthreads();
+                rnorm = ops.ninf(r, sh);
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                rho_1 = rho;
+            }
+        } else {
+            double rho_1 = 0.0, alpha = 0.0, omega = 0.0;
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) { rh[t] = r[t]; p[t] = 0.0; v[t] = 0.0; }
+            __syncthreads();
+            for (int iter = 1; iter <= a.maxiter; ++iter) {
+                const double rho = ops.dot(rh, r, sh);
+                if (rho == 0.0) { ret = 1; break; }
+                if (iter == 1) {
+                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t];
+                } else {
+                    const double beta = (rho / rho_1) * (alpha / omega);
+                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t] + beta * (p[t] - omega * v[t]);
+                }
+                __syncthreads();
+                ops.apply(p, v);
+                const double rhTv = ops.dot(rh, v, sh);
+                if (rhTv != 0.0) alpha = rho / rhTv;
+                else { ret = 2; break; }
+                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * v[t]; }
+                __syncthreads();
+                rnorm = ops.ninf(r, sh);
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                ops.apply(r, tt);
+                const double t_t = ops.dot(tt, tt, sh), t_r = ops.dot(tt, r, sh);
+                if (t_t != 0.0) omega = t_r / t_t;
+                else { ret = 3; break; }
+                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += omega * r[t]; r[t] += -omega * tt[t]; }
+                __syncthreads();
+                rnorm = ops.ninf(r, sh);
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                if (omega == 0.0) { ret = 4; break; }
+                rho_1 = rho;
+            }
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+    }
+    const bool keep = (ret == 0 || ret == 8) && rnorm < rnorm0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = keep ? x[t] + sorig[t] : sorig[t];
+    __syncthreads();
+    // MLMG: on failure the correction is zeroed and nuf smoother calls follow
+    if (ret != 0 && ret != 9) {
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
+        for (int s = 0; s < a.nuf; ++s) ops.smooth(x, b, tmp);
+    }
+}
+
+void launch_bottom(const BottomArgs& a, cudaStream_t st) {
+    dispatch_model<double>(a.P.model, [&](auto m) { k_bottom<decltype(m)::value><<<1, kBottomThreads, 0, st>>>(a); });
+    launched();
+}
+
+}  // namespace ae

@@ -1,0 +1,154 @@
+// Host-side declarations of the kernel launchers shared by the translation units of
+// libaefast.so.  Each launcher is instantiated for R = double and R = float.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "ae_device.cuh"
+
+namespace ae {
+
+// kernels launched by this library (eager launches; graph replays are added by the solver)
+extern std::atomic<long long> g_kernel_launches;
+
+inline Box3 box_grow(Box3 b, int n) {
+    for (int d = 0; d < 3; ++d) { b.lo[d] -= n; b.hi[d] += n; }
+    return b;
+}
+inline Box3 box_isect(const Box3& a, const Box3& b) {
+    Box3 r;
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = a.lo[d] > b.lo[d] ? a.lo[d] : b.lo[d];
+        r.hi[d] = a.hi[d] < b.hi[d] ? a.hi[d] : b.hi[d];
+    }
+    return r;
+}
+inline bool box_empty(const Box3& b) { return b.hi[0] < b.lo[0] || b.hi[1] < b.lo[1] || b.hi[2] < b.lo[2]; }
+inline long long box_npts(const Box3& b) {
+    if (box_empty(b)) return 0;
+    return (long long)(b.hi[0] - b.lo[0] + 1) * (b.hi[1] - b.lo[1] + 1) * (b.hi[2] - b.lo[2] + 1);
+}
+inline bool box_contains(const Box3& outer, const Box3& inner) {
+    for (int d = 0; d < 3; ++d)
+        if (inner.lo[d] < outer.lo[d] || inner.hi[d] > outer.hi[d]) return false;
+    return true;
+}
+inline Box3 geo_domain(const Geo& g) {
+    Box3 b;
+    for (int d = 0; d < 3; ++d) { b.lo[d] = g.dlo[d]; b.hi[d] = g.dhi[d]; }
+    return b;
+}
+inline Box3 geo_valid(const Geo& g) {
+    Box3 b;
+    for (int d = 0; d < 3; ++d) { b.lo[d] = g.vlo[d]; b.hi[d] = g.vhi[d]; }
+    return b;
+}
+inline Box3 geo_store(const Geo& g) { return box_grow(geo_valid(g), g.ng); }
+// Fapply / Diagonal region: valid box grown by 1, clipped to the domain (Elastic.cpp:164-166)
+inline Box3 geo_apply_region(const Geo& g) {
+    return box_isect(box_isect(box_grow(geo_valid(g), 1), geo_domain(g)), geo_store(g));
+}
+
+template <class R>
+SCoef<R> make_scoef(const Geo& g) {
+    SCoef<R> K;
+    for (int d = 0; d < 3; ++d) {
+        K.h[d] = (R)(0.5 / g.dx[d]);
+        K.id[d] = (R)(1.0 / g.dx[d]);
+        K.i2[d] = (R)(1.0 / (g.dx[d] * g.dx[d]));
+        K.bb[d] = (R)(-2.0 / g.dx[d] / g.dx[d]);
+    }
+    K.m01 = (R)(0.25 / (g.dx[0] * g.dx[1]));
+    K.m02 = (R)(0.25 / (g.dx[0] * g.dx[2]));
+    K.m12 = (R)(0.25 / (g.dx[1] * g.dx[2]));
+    return K;
+}
+
+// View over a level's storage box (the layout of every internal array).
+template <class T>
+View<T> level_view(const Geo& g, T* p) {
+    const Box3 s = geo_store(g);
+    View<T> v;
+    v.p = p;
+    for (int d = 0; d < 3; ++d) v.lo[d] = s.lo[d];
+    v.sy = s.hi[0] - s.lo[0] + 1;
+    v.sz = v.sy * (s.hi[1] - s.lo[1] + 1);
+    v.sc = v.sz * (s.hi[2] - s.lo[2] + 1);
+    return v;
+}
+template <class T>
+View<const T> cview(const View<T>& v) {
+    View<const T> c;
+    c.p = v.p;
+    for (int d = 0; d < 3; ++d) c.lo[d] = v.lo[d];
+    c.sy = v.sy; c.sz = v.sz; c.sc = v.sc;
+    return c;
+}
+
+struct OpParams {
+    Geo g;
+    BCP bc;
+    int model;
+    int uniform;
+};
+
+// ------------------------------------------------------------------ launchers
+template <class R>
+void launch_fapply(const OpParams& P, View<const R> C, View<const R> u, View<R> f, cudaStream_t st);
+// r = b - A x over the apply region; if norm != nullptr, atomically max-reduce |r| over
+// valid ∩ domain into *norm (bit pattern of a non-negative double, zero it first);
+// if r32 != nullptr also store (float) r there.
+template <class R>
+void launch_residual(const OpParams& P, View<const R> C, View<const R> x, View<const R> b, View<R> r,
+                     unsigned long long* norm, View<float>* r32, cudaStream_t st);
+// One damped-Jacobi sweep: xo = (1-w) xi + w (b - (A xi - D xi)) / D on grow(valid,1)∩dom,
+// zero on the ring grow(valid,2) \ grow(valid,1), copy elsewhere.
+template <class R>
+void launch_jacobi(const OpParams& P, View<const R> C, View<const R> invD, View<const R> D, View<const R> xi,
+                   View<const R> b, View<R> xo, R omega, cudaStream_t st);
+template <class R>
+void launch_diagonal(const OpParams& P, View<const R> C, View<R> D, View<R> invD, int* nan_flag, cudaStream_t st);
+template <class R>
+void launch_restrict(const Geo& gc, int ncomp, View<R> crse, View<const R> fine, cudaStream_t st);
+template <class R>
+void launch_interp_add(const Geo& gf, int ncomp, View<R> fine, View<const R> crse, cudaStream_t st);
+// region-wise copy/convert: dst(region) = src(region), component by component
+template <class Ro, class Ri>
+void launch_copy(const Box3& region, int ncomp, View<Ro> dst, View<const Ri> src, cudaStream_t st);
+// dst += alpha * src over region
+template <class Ro, class Ri>
+void launch_axpy(const Box3& region, int ncomp, View<Ro> dst, double alpha, View<const Ri> src, cudaStream_t st);
+template <class R>
+void launch_fill(const Box3& region, int ncomp, View<R> dst, R value, cudaStream_t st);
+// max |v| over region into *norm (bit pattern)
+template <class R>
+void launch_norminf(const Box3& region, int ncomp, View<const R> v, unsigned long long* norm, cudaStream_t st);
+void launch_bc_init(const Geo& g, const BCP& bc, const double* val, int homogeneous, View<double> rhs,
+                    cudaStream_t st);
+void launch_strain(const Geo& g, View<const double> u, View<double> e, int voigt, cudaStream_t st);
+void launch_stress(const OpParams& P, View<const double> C, View<const double> u, View<double> s, int voigt,
+                   cudaStream_t st);
+void launch_energy(const OpParams& P, View<const double> C, View<const double> u, View<double> w, cudaStream_t st);
+
+struct BottomArgs {
+    OpParams P;
+    SCoef<double> K;
+    const double* C;
+    const double* D;
+    const double* invD;
+    double* x;
+    const double* b;
+    double* work;  // 8 vectors of 3 * nn doubles
+    long long nn;
+    int bottom;    // 0 CG, 1 BiCGStab
+    int maxiter;
+    double reltol;
+    int nuf;
+    int sweeps;
+    double omega;
+    int* fail_count;  // incremented when the Krylov solve fails
+};
+void launch_bottom(const BottomArgs& a, cudaStream_t st);
+
+}  // namespace ae

@@ -1,0 +1,184 @@
+/*
+ * aefast.h -- C ABI of the GB300 elastic-operator library (libaefast.so).
+ *
+ * This is the drop-in boundary for the reference's nodal linear-elastic solve path:
+ * Operator::Elastic<T> (src/Operator/Elastic.H:20-171), its base
+ * Operator::Operator<Grid::Node> (src/Operator/Operator.H:30-128), the operator
+ * boundary conditions BC::Operator::Elastic<T> (src/BC/Operator/Elastic.H:12-406)
+ * and the Solver::Nonlocal::Linear / Newton<T> drivers
+ * (src/Solver/Nonlocal/Linear.H:19-143, src/Solver/Nonlocal/Newton.H:15-349).
+ * The reference exposes these as C++ virtuals on AMReX types; this header gives the
+ * same operations as plain C entry points over plain pointers and sizes.
+ * include/alamo_elastic.H wraps it back into the reference's class and method names.
+ *
+ * Conventions
+ *  - Every function returns an ae_status (0 = success, negative = error);
+ *    ae_last_error() gives a message for the calling thread.
+ *  - Fields are described by ae_fab, which is the memory layout of an AMReX
+ *    FArrayBox/Array4: index box [lo, hi] (ghost nodes included), i fastest, then j,
+ *    then k, then the component.  Nodal indices; the problem domain starts at 0.
+ *  - Kernel-level entry points (ae_fapply ... ae_interp_add) take DEVICE pointers and
+ *    are ordered on the operator's stream (ae_op_set_stream).  ae_op_set_model and
+ *    ae_solve accept host or device pointers.
+ *  - One operator handle may be used by one host thread at a time; distinct handles
+ *    are independent.
+ */
+#ifndef AEFAST_H
+#define AEFAST_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ae_op_s ae_op;
+
+typedef enum {
+    AE_OK = 0,
+    AE_ERR_ARG = -1,           /* bad argument (sizes, layout, index out of range)         */
+    AE_ERR_NAN = -2,           /* NaN/Inf found (diagonal, residual)                        */
+    AE_ERR_NOT_CONVERGED = -3, /* solver reached max_iter (reference: MLMG aborts)          */
+    AE_ERR_OOM = -4,           /* device allocation failed                                  */
+    AE_ERR_CUDA = -5,          /* CUDA runtime error                                        */
+    AE_ERR_STATE = -6          /* call order violated (e.g. solve before set_model)         */
+} ae_status;
+
+/* Per-node stiffness kinds (Model::Solid::Solid<Sym>::ddw storage).
+ *  ISOTROPIC : 2 coefficients (lambda, mu)        Set::Matrix4<3,Sym::Isotropic>
+ *  MAJORMINOR: 21 coefficients (reference slots)   Set::Matrix4<3,Sym::MajorMinor>
+ *  DIAGONAL  : 9 coefficients A(i,j), row-major    Set::Matrix4<3,Sym::Diagonal>   */
+typedef enum { AE_MODEL_ISOTROPIC = 0, AE_MODEL_MAJORMINOR = 1, AE_MODEL_DIAGONAL = 2 } ae_model_kind;
+
+/* BC::Operator::Elastic<T>::Type, same numbering (src/BC/Operator/Elastic.H:24) */
+typedef enum { AE_BC_DISPLACEMENT = 0, AE_BC_TRACTION = 1, AE_BC_PERIODIC = 2, AE_BC_NEUMANN = 3 } ae_bc_type;
+
+/* Face/edge/corner numbering of BC::Operator::Elastic<T>::Face (src/BC/Operator/Elastic.H:33-41) */
+enum {
+    AE_XLO, AE_YLO, AE_ZLO, AE_XHI, AE_YHI, AE_ZHI,
+    AE_YLO_ZLO, AE_YLO_ZHI, AE_YHI_ZLO, AE_YHI_ZHI,
+    AE_ZLO_XLO, AE_ZLO_XHI, AE_ZHI_XLO, AE_ZHI_XHI,
+    AE_XLO_YLO, AE_XLO_YHI, AE_XHI_YLO, AE_XHI_YHI,
+    AE_XLO_YLO_ZLO, AE_XLO_YLO_ZHI, AE_XLO_YHI_ZLO, AE_XLO_YHI_ZHI,
+    AE_XHI_YLO_ZLO, AE_XHI_YLO_ZHI, AE_XHI_YHI_ZLO, AE_XHI_YHI_ZHI,
+    AE_NFACES
+};
+
+/* One AMR level: a single nodal patch inside the level's problem domain.
+ * Replaces the Geometry/BoxArray pair passed to Operator::Elastic<T>::define
+ * (src/Operator/Elastic.cpp:30-55).  Level l+1 refines level l by 2. */
+typedef struct {
+    int domain_cells[3]; /* cells of the level's problem domain (nodal domain = [0, cells]) */
+    int lo[3], hi[3];    /* nodal valid box of the level's patch (inclusive)                */
+    double dx[3];        /* cell size                                                        */
+} ae_level_desc;
+
+/* Field view in AMReX Array4 layout (see conventions above). */
+typedef struct {
+    void* data;        /* element (lo, comp 0)                                              */
+    int lo[3], hi[3];  /* index box spanned by data (inclusive, ghosts included)            */
+    int ncomp;
+    int is_float;      /* 0: double, 1: float                                               */
+} ae_fab;
+
+/* Solver options: AMReX MLMG knobs set by Solver::Nonlocal::Linear
+ * (src/Solver/Nonlocal/Linear.H:23-29, Parse :121-140). */
+typedef struct {
+    int max_fmg_iter;     /* iterations run as F-cycles before V-cycles (MLMG max_fmg_iter;    
+                             reference default 1e8: always F; 0: always V)                     */
+    int nu1, nu2;         /* smoother calls before/after the coarse correction (MLMG nu1/nu2) */
+    int sweeps;           /* damped-Jacobi sweeps per smoother call (reference Fsmooth: 2)    */
+    int bottom;           /* 0: CG, 1: BiCGStab (reference default)                           */
+    int max_iter;         /* MLMG max_iter                                                    */
+    int bottom_max_iter;  /* MLMG bottom_max_iter                                             */
+    double bottom_reltol; /* MLMG bottom relative tolerance                                   */
+    int nuf;              /* smoother calls after a failed bottom solve                       */
+    int max_mg_levels;    /* cap on multigrid levels (<= 0: coarsen while possible)           */
+    double omega;         /* Jacobi damping (reference: 2/3)                                  */
+    int precision;        /* 0: FP64 throughout; 1: FP32 cycle inside FP64 refinement         */
+    int inner_cycles;     /* precision 1: FP32 cycles per FP64 residual                       */
+    int verbose;
+    int use_graph;        /* capture each iteration in a CUDA graph                           */
+} ae_solver_opts;
+
+typedef struct {
+    int iters;            /* outer iterations (MLMG iterations, or refinement steps)          */
+    int cycles;           /* multigrid cycles executed                                        */
+    int converged;
+    int nlevels;          /* multigrid levels on AMR level 0                                  */
+    int bottom_fail;      /* bottom solves that did not converge (smoother fallback used)     */
+    int pad_;
+    double res0, resfinal, target;
+    double seconds;       /* wall time of the solve call                                      */
+} ae_solve_stats;
+
+const char* ae_last_error(void);
+const char* ae_version(void);
+void ae_default_solver_opts(ae_solver_opts* o);
+
+/* Operator::Elastic<T>::define + Operator<Grid::Node>::define (Elastic.cpp:30-55,
+ * Operator.cpp:215-258): allocates the multigrid hierarchy and the operator diagonal. */
+int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out);
+int ae_op_destroy(ae_op* op);
+/* cudaStream_t passed as void*; NULL selects the operator's own stream, a blocking
+ * stream that is ordered with the legacy default stream. */
+int ae_op_set_stream(ae_op* op, void* stream);
+/* Operator::Elastic<T>::SetModel(amrlev, FabArray) (Elastic.cpp:84-118): ncomp = coefficient count;
+ * the fab must cover the level's valid box grown by 2 clipped to the domain. */
+int ae_op_set_model(ae_op* op, int amrlev, const ae_fab* coeffs);
+/* Operator::Elastic<T>::SetModel(T&) (Elastic.cpp:57-82): one stiffness on every node. */
+int ae_op_set_model_uniform(ae_op* op, const double* coeffs, int ncoef);
+/* BC::Operator::Elastic<T>::Set for all 26 faces (Elastic.H:61-69); val used by ae_bc_init. */
+int ae_op_set_bc(ae_op* op, const int* type /*[26][3]*/, const double* val /*[26][3]*/);
+/* Operator::Elastic<T>::SetUniform / SetHomogeneous (Elastic.H:48,111). */
+int ae_op_set_flags(ae_op* op, int uniform, int homogeneous);
+/* Operator<Grid::Node>::prepareForSolve (Operator.cpp:445-452): stiffness average-down
+ * (Elastic.cpp:620-652,722-809) and Diagonal on every level (Elastic.cpp:264-352). */
+int ae_op_prepare(ae_op* op);
+int ae_op_num_amr_levels(const ae_op* op);
+int ae_op_num_mg_levels(const ae_op* op, int amrlev);
+/* nodal valid box and domain of (amrlev, mglev) */
+int ae_op_level_info(const ae_op* op, int amrlev, int mglev, int lo[3], int hi[3], int dom_hi[3], double dx[3]);
+
+/* Elastic<T>::Fapply (Elastic.cpp:151-260): out = A in over the valid box grown by 1
+ * clipped to the domain.  Device fabs, 3 components. */
+int ae_fapply(ae_op* op, int amrlev, int mglev, const ae_fab* out, const ae_fab* in);
+/* Elastic<T>::Diagonal (Elastic.cpp:264-352) copied out of the operator. */
+int ae_diagonal(ae_op* op, int amrlev, int mglev, const ae_fab* diag);
+/* Operator<Grid::Node>::Fsmooth (Operator.cpp:90-162): nsweeps damped-Jacobi sweeps in place. */
+int ae_fsmooth(ae_op* op, int amrlev, int mglev, const ae_fab* x, const ae_fab* b, int nsweeps, double omega);
+/* Operator<Grid::Node>::correctionResidual / solutionResidual (Operator.cpp:841-863):
+ * r = b - A x; *norm_inf (host) receives the max-norm over the valid box. */
+int ae_residual(ae_op* op, int amrlev, int mglev, const ae_fab* r, const ae_fab* x, const ae_fab* b,
+                double* norm_inf);
+/* Operator<Grid::Node>::restriction (Operator.cpp:454-554): crse on mglev cmglev from fine on cmglev-1. */
+int ae_restrict(ae_op* op, int amrlev, int cmglev, const ae_fab* crse, const ae_fab* fine);
+/* Operator<Grid::Node>::interpolation (Operator.cpp:556-624): fine (mglev fmglev) += I(crse). */
+int ae_interp_add(ae_op* op, int amrlev, int fmglev, const ae_fab* fine, const ae_fab* crse);
+/* BC::Operator::Elastic<T>::Init (BC/Operator/Elastic.H:106-181): BC values into rhs. */
+int ae_bc_init(ae_op* op, int amrlev, const ae_fab* rhs, int homogeneous);
+/* Elastic<T>::Strain / Stress / Energy (Elastic.cpp:399-572), valid box, device fabs. */
+int ae_strain(ae_op* op, int amrlev, const ae_fab* eps, const ae_fab* u, int voigt);
+int ae_stress(ae_op* op, int amrlev, const ae_fab* sig, const ae_fab* u, int voigt);
+int ae_energy(ae_op* op, int amrlev, const ae_fab* w, const ae_fab* u);
+
+/* Solver::Nonlocal::Linear::solve (Linear.H:102-112) -> MLMG::solve.
+ * sol and rhs: one fab per AMR level, host or device; sol holds the initial guess.
+ * Returns AE_ERR_NOT_CONVERGED if max_iter is reached. */
+int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
+             const ae_solver_opts* opts, ae_solve_stats* stats);
+
+/* Device memory of the operator (bytes), for admission control. */
+long long ae_op_device_bytes(const ae_op* op);
+
+/* Instrumentation (no counterpart in the reference, which times with BL_PROFILE scopes).
+ * ae_kernel_launches: kernels this library has launched in the process (graph replays
+ * count every kernel in the graph).  ae_profile_kernel: average CUDA-event duration of
+ * `reps` back-to-back launches of one kernel on the operator's own buffers at
+ * (amrlev, mglev): which = 0 Fapply, 1 Jacobi sweep, 2 residual, 3 restriction to
+ * mglev+1, 4 interpolation from mglev+1; precision 0 = FP64, 1 = FP32. */
+long long ae_kernel_launches(void);
+int ae_profile_kernel(ae_op* op, int which, int amrlev, int mglev, int precision, int reps, double* avg_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

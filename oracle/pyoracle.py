@@ -1,0 +1,224 @@
+"""ctypes front end of the CPU FP64 oracle (test infrastructure only).
+
+Only tests/, the smoke check and bench.py's cpu_baseline leg import this module,
+and only as the checker.  Fields are numpy float64 arrays shaped
+(ncomp, nz, ny, nx) over the stored box grow(valid, ng), i fastest.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ORC_ISOTROPIC, ORC_MAJORMINOR, ORC_DIAGONAL = 0, 1, 2
+NCOEF = {ORC_ISOTROPIC: 2, ORC_MAJORMINOR: 21, ORC_DIAGONAL: 9}
+
+
+class Level(C.Structure):
+    _fields_ = [("dom_lo", C.c_int * 3), ("dom_hi", C.c_int * 3),
+                ("lo", C.c_int * 3), ("hi", C.c_int * 3),
+                ("ng", C.c_int), ("pad_", C.c_int), ("dx", C.c_double * 3)]
+
+    @property
+    def shape(self):
+        return tuple(self.hi[d] - self.lo[d] + 1 + 2 * self.ng for d in (2, 1, 0))
+
+
+class Opts(C.Structure):
+    _fields_ = [("max_fmg_iter", C.c_int), ("nu1", C.c_int), ("nu2", C.c_int), ("sweeps", C.c_int),
+                ("bottom", C.c_int), ("max_iter", C.c_int), ("bottom_max_iter", C.c_int),
+                ("bottom_reltol", C.c_double), ("nuf", C.c_int), ("max_mg_levels", C.c_int),
+                ("omega", C.c_double), ("uniform", C.c_int), ("pad_", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iters", C.c_int), ("converged", C.c_int), ("nlevels", C.c_int),
+                ("bottom_fail", C.c_int), ("res0", C.c_double), ("resfinal", C.c_double),
+                ("target", C.c_double), ("hist", C.c_double * 256)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        _lib = C.CDLL(path)
+        d = C.POINTER(C.c_double)
+        i = C.POINTER(C.c_int)
+        L = C.POINTER(Level)
+        _lib.orc_fapply.argtypes = [L, C.c_int, d, i, C.c_int, d, d]
+        _lib.orc_diagonal.argtypes = [L, C.c_int, d, i, d]
+        _lib.orc_fsmooth.argtypes = [L, C.c_int, d, i, C.c_int, d, d, d, C.c_int, C.c_double]
+        _lib.orc_residual.argtypes = [L, C.c_int, d, i, C.c_int, d, d, d, d]
+        _lib.orc_restrict.argtypes = [L, L, C.c_int, d, d]
+        _lib.orc_interp_add.argtypes = [L, L, C.c_int, d, d]
+        _lib.orc_bc_init.argtypes = [L, i, d, C.c_int, d]
+        _lib.orc_strain.argtypes = [L, d, C.c_int, d]
+        _lib.orc_stress.argtypes = [L, C.c_int, d, d, C.c_int, d]
+        _lib.orc_energy.argtypes = [L, C.c_int, d, d, d]
+        _lib.orc_mm_full.argtypes = [d, d]
+        _lib.orc_mm_stress.argtypes = [d, d, d]
+        _lib.orc_mm_div.argtypes = [d, d, d]
+        _lib.orc_solve.argtypes = [L, C.c_int, d, i, d, d, C.c_double, C.c_double,
+                                   C.POINTER(Opts), C.POINTER(Stats)]
+        _lib.orc_num_mg_levels.argtypes = [L, C.c_int]
+        _lib.orc_set_threads.argtypes = [C.c_int]
+    return _lib
+
+
+def _d(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def level(n, dx=None, lo=(0, 0, 0), hi=None, ng=0, dom_hi=None):
+    """Level over the nodal domain [0, n] per axis (n cells); valid box defaults to the domain."""
+    n = (n, n, n) if np.isscalar(n) else tuple(n)
+    L = Level()
+    dom_hi = n if dom_hi is None else dom_hi
+    hi = dom_hi if hi is None else hi
+    dx = tuple(1.0 / c for c in n) if dx is None else ((dx,) * 3 if np.isscalar(dx) else tuple(dx))
+    for d in range(3):
+        L.dom_lo[d] = 0
+        L.dom_hi[d] = dom_hi[d]
+        L.lo[d] = lo[d]
+        L.hi[d] = hi[d]
+        L.dx[d] = dx[d]
+    L.ng = ng
+    return L
+
+
+def coarsen(L):
+    Lc = Level()
+    for d in range(3):
+        Lc.dom_lo[d] = L.dom_lo[d] // 2
+        Lc.dom_hi[d] = L.dom_hi[d] // 2
+        Lc.lo[d] = L.lo[d] // 2
+        Lc.hi[d] = L.hi[d] // 2
+        Lc.dx[d] = L.dx[d] * 2.0
+    Lc.ng = 0
+    return Lc
+
+
+def fapply(L, model, Cf, bctype, u, uniform=False):
+    f = np.zeros_like(u)
+    bt, bp = _i(bctype)
+    lib().orc_fapply(C.byref(L), model, _d(Cf), bp, int(uniform), _d(u), _d(f))
+    return f
+
+
+def diagonal(L, model, Cf, bctype):
+    D = np.zeros((3,) + L.shape)
+    bt, bp = _i(bctype)
+    lib().orc_diagonal(C.byref(L), model, _d(Cf), bp, _d(D))
+    return D
+
+
+def fsmooth(L, model, Cf, bctype, diag, x, b, nsweeps=2, omega=2.0 / 3.0, uniform=False):
+    x = x.copy()
+    bt, bp = _i(bctype)
+    lib().orc_fsmooth(C.byref(L), model, _d(Cf), bp, int(uniform), _d(diag), _d(x), _d(b), nsweeps, omega)
+    return x
+
+
+def residual(L, model, Cf, bctype, x, b, uniform=False):
+    r = np.zeros_like(x)
+    nrm = C.c_double(0)
+    bt, bp = _i(bctype)
+    lib().orc_residual(C.byref(L), model, _d(Cf), bp, int(uniform), _d(x), _d(b), _d(r), C.byref(nrm))
+    return r, nrm.value
+
+
+def restrict(Lc, Lf, fine):
+    ncomp = fine.shape[0]
+    crse = np.zeros((ncomp,) + Lc.shape)
+    lib().orc_restrict(C.byref(Lc), C.byref(Lf), ncomp, _d(crse), _d(np.ascontiguousarray(fine)))
+    return crse
+
+
+def interp_add(Lf, Lc, fine, crse):
+    fine = fine.copy()
+    lib().orc_interp_add(C.byref(Lf), C.byref(Lc), fine.shape[0], _d(fine), _d(np.ascontiguousarray(crse)))
+    return fine
+
+
+def bc_init(L, bctype, bcval, rhs, homogeneous=False):
+    rhs = rhs.copy()
+    bt, bp = _i(bctype)
+    bv = np.ascontiguousarray(bcval, dtype=np.float64)
+    lib().orc_bc_init(C.byref(L), bp, _d(bv), int(homogeneous), _d(rhs))
+    return rhs
+
+
+def strain(L, u, voigt=False):
+    e = np.zeros((6 if voigt else 9,) + L.shape)
+    lib().orc_strain(C.byref(L), _d(u), int(voigt), _d(e))
+    return e
+
+
+def stress(L, model, Cf, u, voigt=False):
+    s = np.zeros((6 if voigt else 9,) + L.shape)
+    lib().orc_stress(C.byref(L), model, _d(Cf), _d(u), int(voigt), _d(s))
+    return s
+
+
+def energy(L, model, Cf, u):
+    w = np.zeros((1,) + L.shape)
+    lib().orc_energy(C.byref(L), model, _d(Cf), _d(u), _d(w))
+    return w
+
+
+def mm_full(c21):
+    out = np.zeros(81)
+    lib().orc_mm_full(_d(np.ascontiguousarray(c21, dtype=np.float64)), _d(out))
+    return out.reshape(3, 3, 3, 3)
+
+
+def mm_stress(c21, g):
+    s = np.zeros(9)
+    lib().orc_mm_stress(_d(np.ascontiguousarray(c21, dtype=np.float64)),
+                        _d(np.ascontiguousarray(g, dtype=np.float64).reshape(9)), _d(s))
+    return s.reshape(3, 3)
+
+
+def mm_div(c21, b):
+    f = np.zeros(3)
+    lib().orc_mm_div(_d(np.ascontiguousarray(c21, dtype=np.float64)),
+                     _d(np.ascontiguousarray(b, dtype=np.float64).reshape(27)), _d(f))
+    return f
+
+
+def default_opts(**kw):
+    o = Opts()
+    o.max_fmg_iter, o.nu1, o.nu2, o.sweeps = 0, 1, 1, 2
+    o.bottom, o.max_iter, o.bottom_max_iter = 0, 200, 200
+    o.bottom_reltol, o.nuf, o.max_mg_levels = 1e-4, 8, 0
+    o.omega, o.uniform = 2.0 / 3.0, 0
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def solve(L, model, Cf, bctype, u0, b, tol_rel=1e-8, tol_abs=0.0, **kw):
+    u = u0.copy()
+    o = default_opts(**kw)
+    st = Stats()
+    bt, bp = _i(bctype)
+    rc = lib().orc_solve(C.byref(L), model, _d(Cf), bp, _d(u), _d(b), tol_rel, tol_abs, C.byref(o), C.byref(st))
+    return u, st, rc
+
+
+def num_mg_levels(L, max_mg_levels=0):
+    return lib().orc_num_mg_levels(C.byref(L), max_mg_levels)
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))

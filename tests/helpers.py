@@ -1,0 +1,77 @@
+"""Shared builders for the tests: seeded stiffness fields, BC tables and analytic fields."""
+import numpy as np
+
+from anisotropicfracture_gb300 import models
+from anisotropicfracture_gb300.elastic import FACE, FACES, BCElastic
+
+D, T, P, N = 0, 1, 2, 3
+
+
+def random_coeffs(model, shape, rng, smooth=False):
+    """Positive-definite-ish per-node stiffness of the given kind over `shape` (nz, ny, nx)."""
+    if model == models.ISOTROPIC:
+        lam = 1.0 + rng.random(shape)
+        mu = 0.5 + rng.random(shape)
+        return np.ascontiguousarray(np.stack([lam, mu]))
+    if model == models.DIAGONAL:
+        return np.ascontiguousarray(0.5 + rng.random((9,) + shape))
+    Rs = models.random_rotations(4, rng)
+    tabs = models.cubic(1.68, 1.21, 0.75, Rs)  # (4, 21)
+    gid = rng.integers(0, 4, size=shape)
+    C = np.moveaxis(tabs[gid], -1, 0)
+    C = C * (0.8 + 0.4 * rng.random(shape))[None]
+    return np.ascontiguousarray(C)
+
+
+def bc_config0():
+    """Config 0 BCs: u = 0 on z = 0, u = (0, 0, 0.01) on z = 1, traction-free lateral faces;
+    edges and corners touching z = 0 / z = 1 take the z-face type."""
+    bc = BCElastic()
+    for f in FACES:
+        for d in range(3):
+            bc.Set(f, d, D, 0.0)
+    for f in ["XLO", "XHI", "YLO", "YHI", "XLO_YLO", "XLO_YHI", "XHI_YLO", "XHI_YHI"]:
+        for d in range(3):
+            bc.Set(f, d, T, 0.0)
+    for f in FACES:
+        if "ZHI" in f:
+            bc.Set(f, 2, D, 0.01)
+    return bc
+
+
+def bc_random(rng):
+    """Every face/edge/corner and direction gets a random type among displacement,
+    traction and Neumann, and a random value."""
+    bc = BCElastic()
+    bc.type[:] = rng.choice([D, T, N], size=(26, 3))
+    bc.val[:] = rng.standard_normal((26, 3))
+    return bc
+
+
+def bc_uniaxial_x():
+    """BCs of src/Test/Operator/Elastic_UniaxialTest.cpp:205-238 (component 0, 3D)."""
+    bc = BCElastic()
+    X, Y, Z = 0, 1, 2
+    bc.Set("XHI", X, D, 0.1); bc.Set("XHI", Y, N, 0.0); bc.Set("YLO", X, N, 0.0); bc.Set("YHI", X, N, 0.0)
+    bc.Set("XHI_YHI", X, D, 0.1); bc.Set("XHI_YLO", X, D, 0.1)
+    bc.Set("XHI", Z, N, 0.0); bc.Set("ZLO", X, N, 0.0); bc.Set("ZHI", X, N, 0.0)
+    bc.Set("ZHI_XHI", X, D, 0.1); bc.Set("ZLO_XHI", X, D, 0.1)
+    for c in ["XHI_YLO_ZLO", "XHI_YLO_ZHI", "XHI_YHI_ZLO", "XHI_YHI_ZHI"]:
+        bc.Set(c, X, D, 0.1)
+    for e in ["YLO_ZLO", "YLO_ZHI", "YHI_ZLO", "YHI_ZHI"]:
+        bc.Set(e, X, N, 0.0)
+        bc.Set(e, Y, N, 0.0)
+    return bc
+
+
+def node_coords(n, shape=None, dx=None):
+    nz, ny, nx = shape if shape is not None else (n + 1,) * 3
+    dx = 1.0 / n if dx is None else dx
+    z, y, x = np.meshgrid(np.arange(nz) * dx, np.arange(ny) * dx, np.arange(nx) * dx, indexing="ij")
+    return x, y, z
+
+
+def normwise_err(a, ref):
+    """max |a - ref| / max |ref|: the per-node error measured against the field's scale."""
+    s = np.abs(ref).max()
+    return float(np.abs(a - ref).max() / (s if s > 0 else 1.0))
