@@ -85,6 +85,7 @@ struct AmrLevel {
     ae_level_desc desc;
     std::vector<MGLevel> mg;
     double *sol = nullptr, *rhs = nullptr;
+    float *sol32 = nullptr, *rhs32 = nullptr;  // mixed precision: correction and its right-hand side
     bool model_set = false;
 };
 
@@ -261,6 +262,10 @@ void alloc_level_fp32(ae_op* op) {
             L.corhold32 = op->alloc<float>(3 * L.nn);
             L.tmp32 = op->alloc<float>(3 * L.nn);
         }
+    for (auto& A : op->amr) {
+        A.sol32 = op->alloc<float>(3 * A.mg[0].nn);
+        A.rhs32 = op->alloc<float>(3 * A.mg[0].nn);
+    }
     op->have32 = true;
 }
 
@@ -433,52 +438,179 @@ struct Cycle {
     }
 };
 
-// One refinement step of a single-level solve on the stream: cycle, update, residual + norm.
-// Everything here is stream-ordered so it can be captured in a CUDA graph.
-void iteration_body(ae_op* op, const ae_solver_opts& o, bool fcyc) {
-    AmrLevel& A = op->amr[0];
-    MGLevel& L = A.mg[0];
-    cudaStream_t st = op->st;
-    const OpParams P = op->params(L.g);
-    const Box3 s = geo_store(L.g);
-    if (o.precision == 0) {
-        Cycle<double> cy{op, o, A.mg, st};
-        cy.run(fcyc);
-        launch_axpy<double, double>(s, 3, level_view(L.g, A.sol), 1.0, cview(level_view(L.g, L.cor)), st);
-        AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), st));
-        launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
-                                cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm, nullptr, st);
-    } else {
-        Cycle<float> cy{op, o, A.mg, st};
-        const int inner = o.inner_cycles > 0 ? o.inner_cycles : 1;
-        for (int c = 0; c < inner; ++c) {
-            cy.run(fcyc);
-            launch_axpy<double, float>(s, 3, level_view(L.g, A.sol), 1.0, cview(level_view(L.g, L.cor32)), st);
-            if (c + 1 < inner)  // FP32 residual of the correction equation, in place
-                launch_residual<float>(P, cview(level_view(L.g, L.C32)), cview(level_view(L.g, L.cor32)),
-                                       cview(level_view(L.g, L.res32)), level_view(L.g, L.res32), nullptr, nullptr,
-                                       st);
+// ------------------------------------------------------------------ composite multi-level iteration
+// MLMG::oneIter over the AMR levels in precision R (see the file header): fine levels are
+// smoothed only (their single multigrid level is the bottom of their cycle), the fine
+// residual is refluxed onto covered coarse nodes (src/Operator/Operator.cpp:728-839), the
+// coarse correction is interpolated into the fine patch and its ghost nodes, and the fine
+// solution is injected onto covered coarse nodes (src/Operator/Operator.cpp:626-641).
+template <class R>
+struct AmrIter {
+    ae_op* op;
+    const ae_solver_opts& o;
+    cudaStream_t st;
+    std::vector<R*> sol, rhs;  // per AMR level, level storage layout
+
+    int finest() const { return (int)op->amr.size() - 1; }
+    MGLevel& T(int a) { return op->amr[a].mg[0]; }
+    const Geo& G(int a) { return T(a).g; }
+    LevelPtrs<R> P(int a) { return ptrs<R>(T(a)); }
+    View<R> V(int a, R* p) { return level_view(G(a), p); }
+    View<const R> CV(int a, R* p) { return cview(level_view(G(a), p)); }
+    Box3 store_dom(int a) { return box_isect(geo_store(G(a)), geo_domain(G(a))); }
+    Box3 covered(int a) {  // coarse nodes of level a-1 under the patch of level a
+        Box3 b;
+        for (int d = 0; d < 3; ++d) { b.lo[d] = G(a).vlo[d] / 2; b.hi[d] = G(a).vhi[d] / 2; }
+        return box_isect(b, geo_domain(G(a - 1)));
+    }
+    void sol_residual(int a) {
+        launch_residual<R>(op->params(G(a)), CV(a, P(a).C), CV(a, sol[a]), CV(a, rhs[a]), V(a, P(a).res), nullptr,
+                           nullptr, st);
+    }
+    void cor_residual(int a) {  // res = res - A cor, in place
+        launch_residual<R>(op->params(G(a)), CV(a, P(a).C), CV(a, P(a).cor), CV(a, P(a).res), V(a, P(a).res),
+                           nullptr, nullptr, st);
+    }
+    void reflux(int c) {
+        const Box3 r = covered(c + 1);
+        launch_restrict<R>(G(c), 3, V(c, P(c).res), CV(c + 1, P(c + 1).res), st, &r);
+    }
+    void add_cor(int a) { launch_axpy<R, R>(store_dom(a), 3, V(a, sol[a]), 1.0, CV(a, P(a).cor), st); }
+    void mini_cycle(int a) {
+        launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
+        Cycle<R> cy{op, o, op->amr[a].mg, st};
+        for (int i = 0; i < o.nu1 + o.nu2; ++i) cy.smooth(0, P(a).cor, P(a).res);
+    }
+    void interp_cor(int a) {
+        launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
+        const Box3 r = store_dom(a);
+        launch_interp_add<R>(G(a), 3, V(a, P(a).cor), CV(a - 1, P(a - 1).cor), st, &r);
+    }
+    void average_down(int a) { launch_inject<R>(covered(a), 3, V(a - 1, sol[a - 1]), CV(a, sol[a]), st); }
+    // residual of every level, fine residuals refluxed onto covered coarse nodes
+    void ml_residual() {
+        for (int a = finest(); a >= 0; --a) {
+            sol_residual(a);
+            if (a < finest()) reflux(a);
         }
-        AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), st));
-        View<float> r32 = level_view(L.g, L.res32);
-        launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
-                                cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm, &r32, st);
+    }
+    void one_iter(bool fcyc) {
+        const int F = finest();
+        for (int a = F; a >= 1; --a) {
+            mini_cycle(a);
+            add_cor(a);
+            sol_residual(a - 1);  // computeResWithCrseSolFineCor
+            cor_residual(a);
+            reflux(a - 1);
+            if (a != F) launch_copy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), CV(a, P(a).cor), st);
+        }
+        Cycle<R> cy{op, o, op->amr[0].mg, st};
+        cy.run(fcyc);
+        add_cor(0);
+        for (int a = 1; a <= F; ++a) {
+            interp_cor(a);
+            add_cor(a);
+            if (a != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), 1.0, CV(a, P(a).cor), st);
+            cor_residual(a);  // computeResWithCrseCorFineCor
+            mini_cycle(a);
+            add_cor(a);
+            if (a != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).cor), 1.0, CV(a, P(a).corhold), st);
+        }
+        for (int a = F; a >= 1; --a) average_down(a);
+    }
+};
+
+std::vector<double*> sol64(ae_op* op) {
+    std::vector<double*> v;
+    for (auto& A : op->amr) v.push_back(A.sol);
+    return v;
+}
+std::vector<double*> rhs64(ae_op* op) {
+    std::vector<double*> v;
+    for (auto& A : op->amr) v.push_back(A.rhs);
+    return v;
+}
+
+// FP64 composite residual of the current solution and its max-norm (into dnorm[0]); in mixed
+// precision also the FP32 copy that drives the next correction cycle.
+void ml_residual64(ae_op* op, const ae_solver_opts& o) {
+    cudaStream_t st = op->st;
+    AmrIter<double> it{op, o, st, sol64(op), rhs64(op)};
+    AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), st));
+    if (it.finest() == 0) {  // fused residual + norm (+ FP32 copy)
+        MGLevel& L = it.T(0);
+        View<float> r32 = o.precision ? level_view(L.g, L.res32) : View<float>{};
+        launch_residual<double>(op->params(L.g), cview(level_view(L.g, L.C)), it.CV(0, it.sol[0]),
+                                it.CV(0, it.rhs[0]), level_view(L.g, L.res), op->dnorm, o.precision ? &r32 : nullptr,
+                                st);
+        return;
+    }
+    it.ml_residual();
+    for (int a = 0; a <= it.finest(); ++a) {
+        MGLevel& L = it.T(a);
+        launch_norminf<double>(box_isect(geo_valid(L.g), geo_domain(L.g)), 3, cview(level_view(L.g, L.res)),
+                               op->dnorm, st);
+        if (o.precision) {
+            launch_copy<float, double>(geo_store(L.g), 3, level_view(L.g, L.res32), cview(level_view(L.g, L.res)), st);
+            launch_copy<float, float>(geo_store(L.g), 3, level_view(L.g, op->amr[a].rhs32),
+                                      cview(level_view(L.g, L.res32)), st);
+        }
     }
 }
 
-void solve_single(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs, ae_solve_stats* stats) {
-    AmrLevel& A = op->amr[0];
-    MGLevel& L = A.mg[0];
+// One step of the solve on the stream: a composite cycle (FP64), or an FP32 correction cycle
+// added to the FP64 solution (mixed), then the FP64 composite residual and norm.  Everything
+// is stream-ordered so it can be captured in a CUDA graph.
+void iteration_body(ae_op* op, const ae_solver_opts& o, bool fcyc) {
     cudaStream_t st = op->st;
-    const OpParams P = op->params(L.g);
-    const Box3 vreg = box_isect(geo_valid(L.g), geo_domain(L.g));
+    if (o.precision == 0) {
+        AmrIter<double> it{op, o, st, sol64(op), rhs64(op)};
+        it.one_iter(fcyc);
+    } else {
+        std::vector<float*> e, r;
+        for (auto& A : op->amr) { e.push_back(A.sol32); r.push_back(A.rhs32); }
+        AmrIter<float> it{op, o, st, e, r};
+        const int inner = o.inner_cycles > 0 ? o.inner_cycles : 1;
+        if (it.finest() == 0) {
+            MGLevel& L = it.T(0);
+            const OpParams P = op->params(L.g);
+            Cycle<float> cy{op, o, op->amr[0].mg, st};
+            for (int c = 0; c < inner; ++c) {
+                cy.run(fcyc);
+                launch_axpy<double, float>(geo_store(L.g), 3, level_view(L.g, op->amr[0].sol), 1.0,
+                                           cview(level_view(L.g, L.cor32)), st);
+                if (c + 1 < inner)  // FP32 residual of the correction equation, in place
+                    launch_residual<float>(P, cview(level_view(L.g, L.C32)), cview(level_view(L.g, L.cor32)),
+                                           cview(level_view(L.g, L.res32)), level_view(L.g, L.res32), nullptr,
+                                           nullptr, st);
+            }
+        } else {
+            for (int a = 0; a <= it.finest(); ++a) launch_fill<float>(geo_store(it.G(a)), 3, it.V(a, e[a]), 0.f, st);
+            for (int c = 0; c < inner; ++c) {
+                it.one_iter(fcyc);
+                if (c + 1 < inner) it.ml_residual();
+            }
+            for (int a = 0; a <= it.finest(); ++a)
+                launch_axpy<double, float>(it.store_dom(a), 3, level_view(it.G(a), op->amr[a].sol), 1.0,
+                                           it.CV(a, e[a]), st);
+            AmrIter<double> it64{op, o, st, sol64(op), rhs64(op)};
+            for (int a = it.finest(); a >= 1; --a) it64.average_down(a);
+        }
+    }
+    ml_residual64(op, o);
+}
+
+void solve_ml(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs, ae_solve_stats* stats) {
+    AmrLevel& A = op->amr[0];
+    cudaStream_t st = op->st;
     AE_CHECK(cudaMemsetAsync(op->dnorm, 0, 2 * sizeof(unsigned long long), st));
     AE_CHECK(cudaMemsetAsync(op->dflag + 1, 0, sizeof(int), st));
-    launch_norminf<double>(vreg, 3, cview(level_view(L.g, A.rhs)), op->dnorm + 1, st);
-    View<float> r32 = o.precision ? level_view(L.g, L.res32) : View<float>{};
-    launch_residual<double>(P, cview(level_view(L.g, L.C)), cview(level_view(L.g, A.sol)),
-                            cview(level_view(L.g, A.rhs)), level_view(L.g, L.res), op->dnorm,
-                            o.precision ? &r32 : nullptr, st);
+    for (auto& Al : op->amr) {
+        const Geo& g = Al.mg[0].g;
+        launch_norminf<double>(box_isect(geo_valid(g), geo_domain(g)), 3, cview(level_view(g, Al.rhs)), op->dnorm + 1,
+                               st);
+    }
+    ml_residual64(op, o);
     const double res0 = read_norm(op, 0);
     const double bnorm = read_norm(op, 1);
     require(std::isfinite(res0) && std::isfinite(bnorm), "initial residual is NaN or infinite", AE_ERR_NAN);
@@ -959,39 +1091,52 @@ int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, do
         else ae_default_solver_opts(&o);
         require(o.sweeps >= 1 && o.nu1 >= 0 && o.nu2 >= 0 && o.max_iter >= 0, "bad solver options");
         require(o.bottom == 0 || o.bottom == 1, "bottom must be 0 (CG) or 1 (BiCGStab)");
-        require(op->amr.size() == 1, "multi-level AMR solve is not available in this build", AE_ERR_ARG);
         if (!op->prepared) prepare(op);
         if (o.precision) prepare32(op);
-        AmrLevel& A = op->amr[0];
-        MGLevel& L = A.mg[0];
-        const Box3 dom = box_isect(geo_valid(L.g), geo_domain(L.g));
-        check_fab(&sol[0], dom, 3, "solve sol");
-        check_fab(&rhs[0], dom, 3, "solve rhs");
-        require(!sol[0].is_float && !rhs[0].is_float, "solve: double fabs required");
-        const bool sol_dev = is_device_ptr(sol[0].data);
-        View<const double> b = device_view_in(op, rhs[0], 0);
-        launch_copy<double, double>(dom, 3, level_view(L.g, A.rhs), b, op->st);
-        View<const double> x0 = device_view_in(op, sol[0], 1);
-        launch_copy<double, double>(dom, 3, level_view(L.g, A.sol), x0, op->st);
+        const int namr = (int)op->amr.size();
+        // fields: level 0 over its domain, finer levels over the patch and its 2 ghost layers
+        std::vector<Box3> region(namr);
+        for (int a = 0; a < namr; ++a) {
+            const Geo& g = op->amr[a].mg[0].g;
+            region[a] = box_isect(geo_store(g), geo_domain(g));
+            check_fab(&sol[a], region[a], 3, "solve sol");
+            check_fab(&rhs[a], region[a], 3, "solve rhs");
+            require(!sol[a].is_float && !rhs[a].is_float, "solve: double fabs required");
+        }
+        for (int a = 0; a < namr; ++a) {
+            AmrLevel& A = op->amr[a];
+            const Geo& g = A.mg[0].g;
+            launch_copy<double, double>(region[a], 3, level_view(g, A.rhs), device_view_in(op, rhs[a], 0), op->st);
+            launch_copy<double, double>(region[a], 3, level_view(g, A.sol), device_view_in(op, sol[a], 1), op->st);
+        }
         int status = AE_OK;
         std::string msg;
         try {
-            solve_single(op, o, tol_rel, tol_abs, stats);
+            solve_ml(op, o, tol_rel, tol_abs, stats);
         } catch (const ApiErr& e) {
             if (e.code != AE_ERR_NOT_CONVERGED) throw;
             status = e.code;
             msg = e.what();
         }
         // copy the solution out (also when not converged, as MLMG leaves its iterate in sol)
-        if (sol_dev) {
-            launch_copy<double, double>(dom, 3, fab_view<double>(sol[0]), cview(level_view(L.g, A.sol)), op->st);
-        } else {
-            const size_t bytes = sizeof(double) * (size_t)fab_elems(sol[0]);
-            ensure_stage(op->stage2, op->stage2_bytes, bytes);
-            ae_fab d = sol[0];
-            d.data = op->stage2;
-            launch_copy<double, double>(dom, 3, fab_view<double>(d), cview(level_view(L.g, A.sol)), op->st);
-            AE_CHECK(cudaMemcpyAsync(sol[0].data, op->stage2, bytes, cudaMemcpyDeviceToHost, op->st));
+        for (int a = 0; a < namr; ++a) {
+            AmrLevel& A = op->amr[a];
+            const Geo& g = A.mg[0].g;
+            if (is_device_ptr(sol[a].data)) {
+                launch_copy<double, double>(region[a], 3, fab_view<double>(sol[a]), cview(level_view(g, A.sol)),
+                                            op->st);
+            } else {
+                const size_t bytes = sizeof(double) * (size_t)fab_elems(sol[a]);
+                ensure_stage(op->stage2, op->stage2_bytes, bytes);
+                ae_fab d = sol[a];
+                d.data = op->stage2;
+                // keep the caller's values outside the written region (ghosts beyond the domain)
+                const Box3 fb = fab_box(sol[a]);
+                if (!(box_contains(region[a], fb) && sol[a].ncomp == 3))
+                    AE_CHECK(cudaMemcpyAsync(op->stage2, sol[a].data, bytes, cudaMemcpyHostToDevice, op->st));
+                launch_copy<double, double>(region[a], 3, fab_view<double>(d), cview(level_view(g, A.sol)), op->st);
+                AE_CHECK(cudaMemcpyAsync(sol[a].data, op->stage2, bytes, cudaMemcpyDeviceToHost, op->st));
+            }
         }
         AE_CHECK(cudaStreamSynchronize(op->st));
         if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg
             const R rv = b.p[ob + n * b.sc] - v[n];
             r.p[orr + n * r.sc] = rv;
             if (R32) r32.p[r32.at(i, j, k) + n * r32.sc] = (float)rv;
-            if (NORM && inv) mx = fmax(mx, (double)fabs(rv));
+            // a NaN residual reports an infinite norm (fmax alone would drop it)
+            if (NORM && inv) mx = (rv != rv) ? (double)INFINITY : fmax(mx, (double)fabs(rv));
         }
     }
     if (NORM) block_max_atomic(mx, norm);
@@ -277,6 +278,17 @@ __global__ void __launch_bounds__(kBlock) k_interp_add(Reg reg, int ncomp, View<
     }
 }
 
+// nodal average_down (src/Operator/Operator.cpp:631): coarse node I takes fine node 2I
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_inject(Reg reg, int ncomp, View<R> crse, View<const R> fine) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int I, J, Kc;
+    reg_ijk(reg, t, I, J, Kc);
+    const long long oc = crse.at(I, J, Kc), of = fine.at(2 * I, 2 * J, 2 * Kc);
+    for (int n = 0; n < ncomp; ++n) crse.p[oc + n * crse.sc] = fine.p[of + n * fine.sc];
+}
+
 // ------------------------------------------------------------------ elementwise
 template <class Ro, class Ri>
 __global__ void __launch_bounds__(kBlock) k_copy(Reg reg, int ncomp, View<Ro> dst, View<const Ri> src) {
@@ -313,7 +325,10 @@ __global__ void __launch_bounds__(kBlock) k_norminf(Reg reg, int ncomp, View<con
         int i, j, k;
         reg_ijk(reg, t, i, j, k);
         const long long o = v.at(i, j, k);
-        for (int n = 0; n < ncomp; ++n) mx = fmax(mx, (double)fabs(v.p[o + n * v.sc]));
+        for (int n = 0; n < ncomp; ++n) {
+            const R a = v.p[o + n * v.sc];
+            mx = (a != a) ? (double)INFINITY : fmax(mx, (double)fabs(a));
+        }
     }
     block_max_atomic(mx, out);
 }

@@ -109,10 +109,18 @@ void launch_jacobi(const OpParams& P, View<const R> C, View<const R> invD, View<
                    View<const R> b, View<R> xo, R omega, cudaStream_t st);
 template <class R>
 void launch_diagonal(const OpParams& P, View<const R> C, View<R> D, View<R> invD, int* nan_flag, cudaStream_t st);
+// crse = R fine on `region` of coarse nodes (default: coarse valid ∩ domain); the weights
+// depend on where a coarse node sits relative to the coarse domain boundary.
 template <class R>
-void launch_restrict(const Geo& gc, int ncomp, View<R> crse, View<const R> fine, cudaStream_t st);
+void launch_restrict(const Geo& gc, int ncomp, View<R> crse, View<const R> fine, cudaStream_t st,
+                     const Box3* region = nullptr);
+// fine += I crse on `region` of fine nodes (default: fine valid ∩ domain)
 template <class R>
-void launch_interp_add(const Geo& gf, int ncomp, View<R> fine, View<const R> crse, cudaStream_t st);
+void launch_interp_add(const Geo& gf, int ncomp, View<R> fine, View<const R> crse, cudaStream_t st,
+                       const Box3* region = nullptr);
+// crse(I) = fine(2 I) on `region` of coarse nodes (nodal average_down)
+template <class R>
+void launch_inject(const Box3& region, int ncomp, View<R> crse, View<const R> fine, cudaStream_t st);
 // region-wise copy/convert: dst(region) = src(region), component by component
 template <class Ro, class Ri>
 void launch_copy(const Box3& region, int ncomp, View<Ro> dst, View<const Ri> src, cudaStream_t st);

@@ -17,17 +17,34 @@ def node_grid(lo, hi, dx):
     return np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
 
 
-def sphere_inclusion_iso(lo, hi, dx, center=(0.5, 0.5, 0.5), radius=0.25, E_in=10.0, nu_in=0.3, E_out=1.0,
-                         nu_out=0.3):
-    """(lambda, mu) per node, shape (2, nz, ny, nx): inclusion E_in/nu_in inside the sphere."""
+def sphere_indicator(lo, hi, dx, center=(0.5, 0.5, 0.5), radius=0.25, eps=None):
+    """Inclusion order parameter eta in [0, 1].  eps = None: sharp node-in-sphere test
+    (IC::Sphere, src/IC/Sphere.H:72-104).  eps > 0: the diffuse profile of IC::Ellipse,
+    eta = 1/2 - 1/2 erf((x^T A x - 1) / (eps |A x|)) with A = I / r^2 (src/IC/Ellipse.H:70-71)."""
     Z, Y, X = node_grid(lo, hi, dx)
     rsq = (X - center[0]) ** 2 + (Y - center[1]) ** 2 + (Z - center[2]) ** 2
-    inside = rsq < radius * radius
+    if eps is None:
+        return (rsq < radius * radius).astype(np.float64)
+    from scipy.special import erf
+    q = (rsq - radius * radius) / (radius * radius)
+    nrm = np.maximum(np.sqrt(rsq) / (radius * radius), 1e-300)
+    return 0.5 - 0.5 * erf(q / eps / nrm)
+
+
+def sphere_inclusion_iso(lo, hi, dx, center=(0.5, 0.5, 0.5), radius=0.25, E_in=10.0, nu_in=0.3, E_out=1.0,
+                         nu_out=0.3, eps_cells=2.0):
+    """(lambda, mu) per node, shape (2, nz, ny, nx): (1 - eta) matrix + eta inclusion, the
+    mixture the Eshelby integrator forms from its eta field (src/Integrator/Eshelby.H:108-118).
+    eps_cells = interface width in cells (None: sharp).  A sharp 10:1 jump makes the
+    reference's damped-Jacobi smoother diverge (the non-divergence-form grad C term), so the
+    configurations use a 2-cell diffuse interface."""
+    eps = None if eps_cells is None else eps_cells * dx[0]
+    eta = sphere_indicator(lo, hi, dx, center, radius, eps)
     li, mi = models.lame_from_E_nu(E_in, nu_in)
     lo_, mo = models.lame_from_E_nu(E_out, nu_out)
-    out = np.empty((2,) + inside.shape)
-    out[0] = np.where(inside, li, lo_)
-    out[1] = np.where(inside, mi, mo)
+    out = np.empty((2,) + eta.shape)
+    out[0] = (1.0 - eta) * lo_ + eta * li
+    out[1] = (1.0 - eta) * mo + eta * mi
     return out
 
 

@@ -1,0 +1,387 @@
+"""Benchmark of the elastic solve path on GB300.
+
+Workload: the polycrystal configuration the headline metric is quoted on -- 3D nodal linear
+elasticity, 256^3-cell coarse level plus a refined (ratio 2) patch over the central 1/8 of the
+volume (two AMR levels of 257^3 nodes each), cubic C11/C12/C44 = 1.68/1.21/0.75 on 64 seeded
+Voronoi grains with Haar-uniform rotations, u = 0 on z = 0, u_z = 0.01 on z = 1, traction-free
+lateral faces, V-cycle with 2 pre/2 post damped-Jacobi sweeps and a CG bottom solve, to a 1e-8
+relative residual.  One step = one full solve from u = 0 on inputs resident in HBM.
+
+  value        mixed-precision solves/s (FP32 cycle inside FP64 refinement), device-timed
+  fp64         plain FP64 solves/s (same solver, FP64 throughout)
+  e2e          mixed solves/s through ae_solve with pinned HOST buffers (H2D + D2H in the region)
+  roofline     the FP32 fused Jacobi sweep on the finest coarse level (the dominant kernel)
+  cpu_baseline the FP64 oracle (a C++ restatement of the reference's CPU path) on a bounded
+               sample of the same workload, extrapolated to one solve
+
+python bench.py --gpus N --steps K --warmup W [--impl reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "mixed vs FP64 elastic solves/s @1e-8 resid; p50/p99 latency; Fapply HBM GB/s"
+UNIT = "solves/s"
+L2_BYTES = 129 * 2 ** 20
+# FP32 fused Jacobi sweep, cubic 21-coefficient stiffness: x in 12 + b 12 + diag 12 + C 84 + x out 12
+JACOBI32_BYTES_PER_NODE = 132
+FAPPLY64_BYTES_PER_NODE = 216
+# FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
+# matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
+# time to a full solve in the reference arm, which cannot afford a full CPU solve.
+CONFIG1_FP64_ITERS = int(os.environ.get("AE_CONFIG1_ITERS", "0"))
+
+
+def workload(n=256, nseeds=64, seed_points=1, seed_rot=2):
+    """Levels, stiffness and right-hand sides of the two-level polycrystal (host arrays)."""
+    from anisotropicfracture_gb300 import microstructure, models
+    from anisotropicfracture_gb300.elastic import BCElastic
+    levels = [dict(cells=n, lo=0, hi=n, ng=0),
+              dict(cells=2 * n, lo=n // 2, hi=3 * n // 2, ng=2)]
+    seeds = microstructure.voronoi_seeds(nseeds, seed_points)
+    rot = models.random_rotations(nseeds, np.random.default_rng(seed_rot))
+    table = models.cubic(1.68, 1.21, 0.75, rot)
+    bc = BCElastic()
+    for f in ["XLO", "XHI", "YLO", "YHI", "XLO_YLO", "XLO_YHI", "XHI_YLO", "XHI_YHI"]:
+        for d in range(3):
+            bc.Set(f, d, bc.Traction, 0.0)
+    from anisotropicfracture_gb300.elastic import FACES
+    for f in FACES:
+        if "ZHI" in f:
+            bc.Set(f, 2, bc.Displacement, 0.01)
+    out = []
+    for L in levels:
+        dx = 1.0 / L["cells"]
+        lo = [L["lo"] - L["ng"]] * 3
+        hi = [L["hi"] + L["ng"]] * 3
+        gid = microstructure.voronoi_grain_ids(lo, hi, (dx, dx, dx), seeds)
+        Cf = np.ascontiguousarray(np.moveaxis(table[gid].astype(np.float64), -1, 0))
+        del gid
+        out.append(dict(L, dx=dx, store_lo=lo, store_hi=hi, C=Cf))
+    return out, bc
+
+
+def level_shape(level):
+    return tuple(level["store_hi"][d] - level["store_lo"][d] + 1 for d in (2, 1, 0))
+
+
+def oracle_level(level):
+    from oracle import pyoracle as po
+    return po.level(level["cells"], lo=(level["lo"],) * 3, hi=(level["hi"],) * 3, ng=level["ng"])
+
+
+def oracle_rhs(level, bc):
+    """BC values on domain-boundary nodes (BC::Operator::Elastic::Init), zero elsewhere; CPU."""
+    from oracle import pyoracle as po
+    return po.bc_init(oracle_level(level), bc.type, bc.val, np.zeros((3,) + level_shape(level)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_oracle_sample(levels, bc, n_iters_solve, sample_iters=1, threads=None, rhs=None):
+    """Time the FP64 oracle on the full workload: set-up plus `sample_iters` composite
+    iterations; extrapolate to a solve of `n_iters_solve` iterations."""
+    from oracle import pyoracle as po
+    if threads:
+        po.set_threads(threads)
+    Ls, Cs, us, bs = [], [], [], []
+    for a, L in enumerate(levels):
+        Ls.append(oracle_level(L))
+        Cs.append(L["C"])
+        bs.append(rhs[a] if rhs is not None else oracle_rhs(L, bc))
+        us.append(np.zeros_like(bs[-1]))
+    t0 = time.perf_counter()
+    po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, us, bs, 1e-30, 0.0, max_iter=0)
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, us, bs, 1e-30, 0.0, max_iter=sample_iters)
+    t_iters = time.perf_counter() - t0 - t_setup
+    t_iter = max(t_iters, 1e-9) / sample_iters
+    t_solve = t_setup + n_iters_solve * t_iter
+    return dict(value=1.0 / t_solve, unit=UNIT, cores=po.lib().orc_num_threads(), kind="port",
+                sample="FP64 oracle on the full two-level 257^3 workload: set-up %.1f s + %d composite "
+                       "iteration(s) at %.2f s each, extrapolated to the %d iterations a solve needs"
+                       % (t_setup, sample_iters, t_iter, n_iters_solve))
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference's CPU path (its C++ restatement in oracle/, the reference
+    itself needs AMReX/Eigen/MPI, absent here) timed on the host cores."""
+    if rank != 0:
+        return
+    levels, bc = workload(args.cells)
+    iters = CONFIG1_FP64_ITERS or args.ref_iters
+    rhs = [oracle_rhs(L, bc) for L in levels]
+    samples = []
+    for k in range(args.warmup + args.steps):
+        cb = cpu_oracle_sample(levels, bc, iters, sample_iters=1, rhs=rhs)
+        if k >= args.warmup:
+            samples.append(1.0 / cb["value"])
+    t = float(np.mean(samples))
+    v = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "polycrystal 2-level AMR, 257^3 + 257^3-node patch, cubic 64 grains",
+                       "precision": "fp64", "cycle": "V(2,2) Jacobi, CG bottom", "tol_rel": 1e-8},
+            "cpu_baseline": dict(cb, value=v),
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-iters", type=int, default=100)
+    ap.add_argument("--cpu-sample-iters", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from anisotropicfracture_gb300 import _lib, build as libbuild, models
+    from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    libbuild.build()
+    lib = _lib.load()
+
+    levels, bc = workload(args.cells)
+    descs = [level_desc(L["cells"], lo=(L["lo"],) * 3, hi=(L["hi"],) * 3) for L in levels]
+    op = Elastic(descs, models.MAJORMINOR)
+    for a, L in enumerate(levels):
+        op.SetModel(a, Field(L["C"], tuple(L["store_lo"])))
+    op.SetBC(bc)
+    op.SetUniform(False)
+    op.prepareForSolve()
+    stream = torch.cuda.Stream()
+    op.set_stream(stream.cuda_stream)
+    dev = torch.device("cuda", local)
+    rhs_d = [torch.zeros((3,) + level_shape(L), dtype=torch.float64, device=dev) for L in levels]
+    for a, L in enumerate(levels):  # BC::Operator::Elastic::Init through the library
+        op.BCInit(a, Field(rhs_d[a], tuple(L["store_lo"])))
+    torch.cuda.synchronize()
+    rhs_h = [b.cpu().numpy() for b in rhs_d]
+    sol_d = [torch.zeros_like(b) for b in rhs_d]
+    nodes = sum(int(np.prod(b.shape[1:])) for b in rhs_h)
+
+    solver = Linear(op)
+    solver.setMaxFmgIter(0)
+    solver.setBottomSolver("cg")
+    solver.setPreSmooth(1)
+    solver.setPostSmooth(1)
+    solver.opts.max_iter = 400
+
+    def fields(xs, rs):
+        return ([Field(x, tuple(L["store_lo"])) for x, L in zip(xs, levels)],
+                [Field(r, tuple(L["store_lo"])) for r, L in zip(rs, levels)])
+
+    def solve_device(prec):
+        solver.setPrecision(prec)
+        with torch.cuda.stream(stream):
+            for x in sol_d:
+                x.zero_()
+        xs, rs = fields(sol_d, rhs_d)
+        solver.solve(xs, rs, 1e-8, 0.0)
+        return solver.stats
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(prec, steps):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = None
+        for _ in range(steps):
+            st = solve_device(prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, st
+
+    # warm-up (mixed is the headline; one FP64 warm-up as well)
+    for _ in range(args.warmup):
+        solve_device("mixed")
+    iters_mixed = solver.stats.iters
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = lib.ae_kernel_launches()
+    ms_mixed, st_mixed = timed("mixed", args.steps)
+    launches = lib.ae_kernel_launches() - l0
+    clk = clocks.stop()
+    res_mixed = (st_mixed.iters, st_mixed.resfinal, st_mixed.target, st_mixed.converged)
+    x_mixed = [x.cpu().numpy() for x in sol_d]
+
+    # FP64 reference solve of the same problem (also the displacement-error yardstick)
+    ms_fp64, fp64_iters, disp_err = None, None, None
+    if args.fp64_steps > 0:
+        solve_device("fp64")
+        ms_fp64, st64 = timed("fp64", args.fp64_steps)
+        fp64_iters = st64.iters
+        x64 = [x.cpu().numpy() for x in sol_d]
+        scale = max(np.abs(x).max() for x in x64)
+        disp_err = max(float(np.abs(a - b).max()) for a, b in zip(x_mixed, x64)) / scale
+
+    # end to end through the C ABI with pinned host buffers
+    solver.setPrecision("mixed")
+    rhs_p = [torch.from_numpy(b).pin_memory() for b in rhs_h]
+    sol_p = [torch.zeros_like(b).pin_memory() for b in rhs_p]
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for x in sol_p:
+            x.zero_()
+        xs, rs = fields([x.numpy() for x in sol_p], [r.numpy() for r in rhs_p])
+        solver.solve(xs, rs, 1e-8, 0.0)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    h2d = sum(b.numel() * 8 for b in rhs_p) * 2  # rhs and initial guess
+    d2h = sum(b.numel() * 8 for b in sol_p)
+
+    # roofline of the dominant kernel: FP32 fused Jacobi sweep on the finest coarse level
+    ms_jac = C.c_double(0.0)
+    _lib.check(lib.ae_profile_kernel(op.handle, 1, 0, 0, 1, 20, C.byref(ms_jac)))
+    ms_f64 = C.c_double(0.0)
+    _lib.check(lib.ae_profile_kernel(op.handle, 0, 0, 0, 0, 5, C.byref(ms_f64)))
+    ms_f32 = C.c_double(0.0)
+    _lib.check(lib.ae_profile_kernel(op.handle, 0, 0, 0, 1, 20, C.byref(ms_f32)))
+    n0 = int(np.prod(rhs_h[0].shape[1:]))
+    peak, peak_kind = measured_peaks()
+    jac_gbs = JACOBI32_BYTES_PER_NODE * n0 / (ms_jac.value * 1e-3) / 1e9
+    fapply64_gbs = FAPPLY64_BYTES_PER_NODE * n0 / (ms_f64.value * 1e-3) / 1e9
+    fapply32_gbs = 108 * n0 / (ms_f32.value * 1e-3) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_oracle_sample(levels, bc, fp64_iters or iters_mixed, sample_iters=args.cpu_sample_iters,
+                                    rhs=rhs_h)
+        except Exception as e:  # pragma: no cover
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: %s" % e}
+
+    value = world * 1000.0 / ms_mixed
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "polycrystal 2-level AMR: 256^3 cells + ratio-2 patch over the central 1/8 "
+                               "(2 x 257^3 nodes), cubic 1.68/1.21/0.75, 64 Voronoi grains",
+                   "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, CG bottom", "tol_rel": 1e-8,
+                   "precision": "mixed: FP32 cycle in FP64 refinement", "nodes": nodes,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (stiffness %.1f GB)" % (sum(L["C"].nbytes for L in levels) / 1e9)},
+        "iters_mixed": res_mixed[0], "resfinal_mixed": res_mixed[1], "target": res_mixed[2],
+        "converged": bool(res_mixed[3]),
+        "fp64": {"value": (world * 1000.0 / ms_fp64) if ms_fp64 else None, "unit": UNIT,
+                 "ms_per_solve": ms_fp64, "iters": fp64_iters},
+        "mixed_over_fp64": (ms_fp64 / ms_mixed) if ms_fp64 else None,
+        "displacement_err_mixed_vs_fp64": disp_err,
+        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "FP32 fused Jacobi sweep (cubic), coarse level 257^3",
+                     "achieved": jac_gbs, "peak": peak, "unit": "GB/s", "frac": jac_gbs / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "bytes_per_node": JACOBI32_BYTES_PER_NODE, "ms_per_launch": ms_jac.value},
+        "fapply": {"fp64_gbs": fapply64_gbs, "fp64_ms": ms_f64.value, "fp32_gbs": fapply32_gbs,
+                   "fp32_ms": ms_f32.value, "bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
+                   "bytes_per_node_fp32": 108},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    op.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

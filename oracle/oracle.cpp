@@ -380,9 +380,13 @@ double residual(const Lev& L, int model, const double* C, const int* bctype, int
 
 // ---------------------------------------------------------------- restriction / interpolation
 // src/Operator/Operator.cpp:486-543 (nodal full weighting, reduced on the domain boundary).
-// The same weights restrict the stiffness field, src/Operator/Elastic.cpp:759-803.
+// The same weights restrict the stiffness field, src/Operator/Elastic.cpp:759-803, and the
+// fine residual onto covered coarse nodes in reflux, src/Operator/Operator.cpp:776-824.
+void restrict_box(const Lev& Lc, const Lev& Lf, int ncomp, double* crse, const double* fine, const Box& bx);
 void restrict_(const Lev& Lc, const Lev& Lf, int ncomp, double* crse, const double* fine) {
-    const Box bx = isect(Lc.valid, Lc.dom);
+    restrict_box(Lc, Lf, ncomp, crse, fine, isect(Lc.valid, Lc.dom));
+}
+void restrict_box(const Lev& Lc, const Lev& Lf, int ncomp, double* crse, const double* fine, const Box& bx) {
     const Box& cd = Lc.dom;
     for (int n = 0; n < ncomp; ++n) {
         for_box(bx, [&](int I, int J, int K) {
@@ -426,8 +430,11 @@ void restrict_(const Lev& Lc, const Lev& Lf, int ncomp, double* crse, const doub
 }
 
 // src/Operator/Operator.cpp:556-624 (trilinear nodal prolongation, added into fine)
+void interp_add_box(const Lev& Lf, const Lev& Lc, int ncomp, double* fine, const double* crse, const Box& bx);
 void interp_add(const Lev& Lf, const Lev& Lc, int ncomp, double* fine, const double* crse) {
-    const Box bx = isect(Lf.valid, Lf.dom);
+    interp_add_box(Lf, Lc, ncomp, fine, crse, isect(Lf.valid, Lf.dom));
+}
+void interp_add_box(const Lev& Lf, const Lev& Lc, int ncomp, double* fine, const double* crse, const Box& bx) {
     for (int n = 0; n < ncomp; ++n) {
         for_box(bx, [&](int i, int j, int k) {
             const double* C0 = crse + n * Lc.nn;
@@ -608,6 +615,127 @@ struct Solver {
             vcycle(m);
             for (size_t i = 0; i < lv[m].cor.size(); ++i) lv[m].cor[i] += lv[m].corhold[i];
         }
+    }
+};
+
+// ---------------------------------------------------------------- composite multi-level solve
+// MLMG::oneIter over AMR levels with the reference's nodal pieces: per fine level a
+// smoother-only cycle (miniCycle), fine correction residuals, reflux of the fine residual
+// onto covered coarse nodes (src/Operator/Operator.cpp:728-839), trilinear interpolation of
+// the coarse correction into the fine patch and its ghost nodes, and injection of the fine
+// solution onto covered coarse nodes (averageDownSolutionRHS, src/Operator/Operator.cpp:626-641).
+struct FineLevel {
+    orc_level ol;
+    Lev* L = nullptr;
+    std::vector<double> C, D, res, cor, rescor, corhold;
+    double* sol = nullptr;
+    const double* rhs = nullptr;
+};
+
+Box covered_by(const Lev& Lf) {
+    Box b;
+    for (int d = 0; d < 3; ++d) { b.lo[d] = Lf.valid.lo[d] / 2; b.hi[d] = Lf.valid.hi[d] / 2; }
+    return b;
+}
+
+struct Amr {
+    Solver* S = nullptr;
+    std::vector<FineLevel> F;
+    double* sol0 = nullptr;
+    const double* rhs0 = nullptr;
+    int finest() const { return (int)F.size(); }
+    Lev& L(int a) { return a == 0 ? *S->lv[0].L : *F[a - 1].L; }
+    double* res(int a) { return a == 0 ? S->lv[0].res.data() : F[a - 1].res.data(); }
+    double* cor(int a) { return a == 0 ? S->lv[0].cor.data() : F[a - 1].cor.data(); }
+    double* sol(int a) { return a == 0 ? sol0 : F[a - 1].sol; }
+    const double* rhs(int a) { return a == 0 ? rhs0 : F[a - 1].rhs; }
+    const double* C(int a) { return a == 0 ? S->lv[0].C.data() : F[a - 1].C.data(); }
+    long N(int a) { return 3 * L(a).nn; }
+
+    void mini_cycle(int a) {
+        FineLevel& f = F[a - 1];
+        std::fill(f.cor.begin(), f.cor.end(), 0.0);
+        for (int i = 0; i < S->o.nu1 + S->o.nu2; ++i)
+            fsmooth(*f.L, S->model, f.C.data(), S->bctype, S->uniform, f.D.data(), f.cor.data(), f.res.data(),
+                    S->o.sweeps, S->o.omega);
+    }
+    void sol_residual(int a) { residual(L(a), S->model, C(a), S->bctype, S->uniform, sol(a), rhs(a), res(a)); }
+    void cor_residual(int a) {
+        FineLevel& f = F[a - 1];
+        residual(*f.L, S->model, f.C.data(), S->bctype, S->uniform, f.cor.data(), f.res.data(), f.rescor.data());
+        const Box r = isect(grow(f.L->valid, 1), isect(f.L->dom, f.L->store));
+        for (int n = 0; n < 3; ++n)
+            for_box(r, [&](int i, int j, int k) {
+                const long c = n * f.L->nn + f.L->at(i, j, k);
+                f.res[c] = f.rescor[c];
+            });
+    }
+    void reflux(int c) { restrict_box(L(c), L(c + 1), 3, res(c), res(c + 1), isect(covered_by(L(c + 1)), L(c).dom)); }
+    void add(int a, const double* x) {
+        double* s = sol(a);
+        for (long i = 0; i < N(a); ++i) s[i] += x[i];
+    }
+    void interp_cor(int a) {
+        FineLevel& f = F[a - 1];
+        std::fill(f.cor.begin(), f.cor.end(), 0.0);
+        interp_add_box(*f.L, L(a - 1), 3, f.cor.data(), cor(a - 1), isect(f.L->store, f.L->dom));
+    }
+    void average_down(int a) {
+        Lev& Lc = L(a - 1);
+        Lev& Lf = L(a);
+        const Box r = isect(covered_by(Lf), Lc.dom);
+        double* sc = sol(a - 1);
+        const double* sf = sol(a);
+        for (int n = 0; n < 3; ++n)
+            for_box(r, [&](int I, int J, int K) {
+                sc[n * Lc.nn + Lc.at(I, J, K)] = sf[n * Lf.nn + Lf.at(2 * I, 2 * J, 2 * K)];
+            });
+    }
+    double norm(int a, const double* v) {
+        Lev& l = L(a);
+        const Box r = isect(l.valid, l.dom);
+        double m = 0;
+        for (int n = 0; n < 3; ++n)
+            for (int k = r.lo[2]; k <= r.hi[2]; ++k)
+                for (int j = r.lo[1]; j <= r.hi[1]; ++j)
+                    for (int i = r.lo[0]; i <= r.hi[0]; ++i) m = std::max(m, std::fabs(v[n * l.nn + l.at(i, j, k)]));
+        return m;
+    }
+    // MLMG::computeMLResidual + composite max-norm
+    double ml_residual() {
+        double m = 0;
+        for (int a = finest(); a >= 0; --a) {
+            sol_residual(a);
+            if (a < finest()) reflux(a);
+        }
+        for (int a = 0; a <= finest(); ++a) m = std::max(m, norm(a, res(a)));
+        return m;
+    }
+    void one_iter(int it) {
+        for (int a = finest(); a >= 1; --a) {
+            mini_cycle(a);
+            add(a, cor(a));
+            sol_residual(a - 1);  // computeResWithCrseSolFineCor
+            cor_residual(a);
+            reflux(a - 1);
+            if (a != finest()) F[a - 1].corhold = F[a - 1].cor;
+        }
+        if (it < S->o.max_fmg_iter) S->fcycle();
+        else S->vcycle(0);
+        add(0, cor(0));
+        for (int a = 1; a <= finest(); ++a) {
+            FineLevel& f = F[a - 1];
+            interp_cor(a);
+            add(a, cor(a));
+            if (a != finest())
+                for (size_t i = 0; i < f.cor.size(); ++i) f.corhold[i] += f.cor[i];
+            cor_residual(a);  // computeResWithCrseCorFineCor
+            mini_cycle(a);
+            add(a, cor(a));
+            if (a != finest())
+                for (size_t i = 0; i < f.cor.size(); ++i) f.cor[i] += f.corhold[i];
+        }
+        for (int a = finest(); a >= 1; --a) average_down(a);
     }
 };
 
@@ -821,11 +949,19 @@ int orc_num_mg_levels(const orc_level* L, int max_mg_levels) {
     return n;
 }
 
-// MLMG::solve restated (single AMR level): convergence when ||r||_inf <= max(tol_abs, tol_rel * max_norm),
-// max_norm = ||b||_inf if ||b||_inf >= ||r0||_inf else ||r0||_inf.
-int orc_solve(const orc_level* L0, int model, const double* C, const int* bctype, double* u, const double* b,
-              double tol_rel, double tol_abs, const orc_opts* opts, orc_stats* stats) {
-    if (L0->ng != 0) return -1;
+// MLMG::solve restated: convergence when the composite ||r||_inf <= max(tol_abs, tol_rel * max_norm),
+// max_norm = ||b||_inf if ||b||_inf >= ||r0||_inf else ||r0||_inf.  Ls[0] covers its domain
+// (ng = 0); Ls[l >= 1] are nested patches refined by 2 with ng = 2.
+int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
+                  double* const* us, const double* const* bs, double tol_rel, double tol_abs, const orc_opts* opts,
+                  orc_stats* stats) {
+    const orc_level* L0 = &Ls[0];
+    if (L0->ng != 0 || namr < 1) return -1;
+    for (int a = 1; a < namr; ++a)
+        if (Ls[a].ng != 2) return -1;
+    const double* C = Cs[0];
+    double* u = us[0];
+    const double* b = bs[0];
     Solver S;
     S.model = model;
     S.nc = ncoef_of(model);
@@ -855,23 +991,45 @@ int orc_solve(const orc_level* L0, int model, const double* C, const int* bctype
     for (int m = 1; m < nlev; ++m) restrict_(*S.lv[m].L, *S.lv[m - 1].L, S.nc, S.lv[m].C.data(), S.lv[m - 1].C.data());
     for (int m = 0; m < nlev; ++m) diagonal(*S.lv[m].L, model, S.lv[m].C.data(), bctype, S.lv[m].D.data());
 
-    const Lev& L = *S.lv[0].L;
-    const long N = 3 * L.nn;
-    const double res0 = residual(L, model, S.lv[0].C.data(), bctype, S.uniform, u, b, S.lv[0].res.data());
+    Amr A;
+    A.S = &S;
+    A.sol0 = u;
+    A.rhs0 = b;
+    A.F.resize(namr - 1);
+    for (int a = 1; a < namr; ++a) {
+        FineLevel& f = A.F[a - 1];
+        f.ol = Ls[a];
+        f.L = new Lev(f.ol);
+        const long nn = f.L->nn;
+        f.C.assign(Cs[a], Cs[a] + S.nc * nn);
+        f.D.assign(3 * nn, 0.0);
+        f.res.assign(3 * nn, 0.0);
+        f.cor.assign(3 * nn, 0.0);
+        f.rescor.assign(3 * nn, 0.0);
+        f.corhold.assign(3 * nn, 0.0);
+        f.sol = us[a];
+        f.rhs = bs[a];
+        diagonal(*f.L, model, f.C.data(), bctype, f.D.data());
+    }
+    struct Cleanup {
+        Amr& A;
+        ~Cleanup() { for (auto& f : A.F) delete f.L; }
+    } cleanup{A};
+
     double bnorm = 0;
-    for (long i = 0; i < N; ++i) bnorm = std::max(bnorm, std::fabs(b[i]));
+    for (int a = 0; a < namr; ++a) bnorm = std::max(bnorm, A.norm(a, A.rhs(a)));
+    const double res0 = A.ml_residual();
     const double max_norm = (bnorm >= res0) ? bnorm : res0;
     const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
     int iters = 0, conv = 0;
     double rn = res0;
     if (res0 <= target) conv = 1;
     for (int it = 0; !conv && it < opts->max_iter; ++it) {
-        if (it < opts->max_fmg_iter) S.fcycle();
-        else S.vcycle(0);
-        for (long i = 0; i < N; ++i) u[i] += S.lv[0].cor[i];
-        rn = residual(L, model, S.lv[0].C.data(), bctype, S.uniform, u, b, S.lv[0].res.data());
+        A.one_iter(it);
+        rn = A.ml_residual();
         if (stats && it < 256) stats->hist[it] = rn;
         iters = it + 1;
+        if (!(rn == rn)) break;
         if (rn <= target) conv = 1;
     }
     if (stats) {
@@ -884,6 +1042,14 @@ int orc_solve(const orc_level* L0, int model, const double* C, const int* bctype
         stats->target = target;
     }
     return conv ? 0 : 1;
+}
+
+int orc_solve(const orc_level* L0, int model, const double* C, const int* bctype, double* u, const double* b,
+              double tol_rel, double tol_abs, const orc_opts* opts, orc_stats* stats) {
+    const double* Cs[1] = {C};
+    double* us[1] = {u};
+    const double* bs[1] = {b};
+    return orc_solve_amr(L0, 1, model, Cs, bctype, us, bs, tol_rel, tol_abs, opts, stats);
 }
 
 }  // extern "C"

@@ -222,3 +222,44 @@ def num_mg_levels(L, max_mg_levels=0):
 
 def set_threads(n):
     lib().orc_set_threads(int(n))
+
+
+def solve_amr(Ls, model, Cs, bctype, us, bs, tol_rel=1e-8, tol_abs=0.0, **kw):
+    """Composite solve over AMR levels; us are updated copies returned as a list."""
+    n = len(Ls)
+    lib().orc_solve_amr.argtypes = [C.POINTER(Level), C.c_int, C.c_int, C.POINTER(C.POINTER(C.c_double)),
+                                    C.POINTER(C.c_int), C.POINTER(C.POINTER(C.c_double)),
+                                    C.POINTER(C.POINTER(C.c_double)), C.c_double, C.c_double,
+                                    C.POINTER(Opts), C.POINTER(Stats)]
+    La = (Level * n)(*Ls)
+    us = [u.copy() for u in us]
+    Cs = [np.ascontiguousarray(c) for c in Cs]
+    bs = [np.ascontiguousarray(b) for b in bs]
+    Cp = (C.POINTER(C.c_double) * n)(*[_d(c) for c in Cs])
+    up = (C.POINTER(C.c_double) * n)(*[_d(u) for u in us])
+    bp = (C.POINTER(C.c_double) * n)(*[_d(b) for b in bs])
+    o = default_opts(**kw)
+    st = Stats()
+    bt, btp = _i(bctype)
+    rc = lib().orc_solve_amr(La, n, model, Cp, btp, up, bp, tol_rel, tol_abs, C.byref(o), C.byref(st))
+    return us, st, rc
+
+
+def amr_levels(n, nlev, shrink=4):
+    """Levels of the reference's test hierarchy (src/Test/Operator/Elastic.cpp:59-92): level 0
+    n^3 cells on the unit cube; each finer level refines the central half of the previous one."""
+    Ls = [level(n)]
+    lo, hi = 0, n  # cell box of the previous level's patch, its own index space
+    for l in range(1, nlev):
+        cells = n * 2 ** l
+        clo, chi = lo + (hi - lo) // shrink, hi - (hi - lo) // shrink
+        lo, hi = 2 * clo, 2 * chi
+        Ls.append(level(cells, lo=(lo,) * 3, hi=(hi,) * 3, ng=2))
+    return Ls
+
+
+def node_coords(L):
+    """x, y, z of every stored node of a level (arrays shaped like one component)."""
+    ax = [(np.arange(L.lo[d] - L.ng, L.hi[d] + L.ng + 1)) * L.dx[d] for d in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return X, Y, Z

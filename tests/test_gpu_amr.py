@@ -1,0 +1,98 @@
+"""Composite multi-level (AMR) solves on the GPU vs the oracle's composite restatement."""
+import numpy as np
+import pytest
+
+from anisotropicfracture_gb300 import microstructure, models
+from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
+from helpers import bc_config0, normwise_err
+from oracle import pyoracle as po
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def descs(Ls):
+    out = []
+    for L in Ls:
+        cells = tuple(L.dom_hi[d] for d in range(3))
+        out.append(level_desc(cells, lo=tuple(L.lo), hi=tuple(L.hi), dx=tuple(L.dx)))
+    return out
+
+
+def lo_of(L):
+    return tuple(L.lo[d] - L.ng for d in range(3))
+
+
+def gpu_amr_solve(Ls, model, Cs, bc, bs, precision="fp64", fmg=0, bottom=0, nu=1, tol=1e-8):
+    op = Elastic(descs(Ls), model)
+    for a, L in enumerate(Ls):
+        op.SetModel(a, Field(Cs[a], lo_of(L)))
+    op.SetBC(bc)
+    op.SetUniform(False)
+    s = Linear(op)
+    s.setMaxFmgIter(fmg)
+    s.opts.bottom, s.opts.nu1, s.opts.nu2 = bottom, nu, nu
+    s.setPrecision(precision)
+    xs = [np.zeros_like(b) for b in bs]
+    s.solve([Field(x, lo_of(L)) for x, L in zip(xs, Ls)], [Field(b, lo_of(L)) for b, L in zip(bs, Ls)], tol, 0.0)
+    return xs, s.stats
+
+
+def polycrystal_amr(n=16, nlev=2, seed=1):
+    Ls = po.amr_levels(n, nlev)
+    bc = bc_config0()
+    seeds = microstructure.voronoi_seeds(8, seed)
+    rot = models.random_rotations(8, np.random.default_rng(seed + 1))
+    tab = models.cubic(1.68, 1.21, 0.75, rot)
+    Cs, bs = [], []
+    for L in Ls:
+        lo = [L.lo[d] - L.ng for d in range(3)]
+        hi = [L.hi[d] + L.ng for d in range(3)]
+        gid = microstructure.voronoi_grain_ids(lo, hi, tuple(L.dx), seeds)
+        Cs.append(np.ascontiguousarray(np.moveaxis(tab[gid], -1, 0)))
+        bs.append(po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)))
+    return Ls, Cs, bc, bs
+
+
+@pytest.mark.parametrize("nlev", [2, 3])
+def test_amr_polycrystal_fp64_matches_oracle(nlev):
+    Ls, Cs, bc, bs = polycrystal_amr(16, nlev)
+    ref, st, rc = po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, [np.zeros_like(b) for b in bs], bs, 1e-8, 0.0)
+    assert rc == 0
+    xs, stats = gpu_amr_solve(Ls, models.MAJORMINOR, Cs, bc, bs)
+    assert stats.converged and abs(stats.iters - st.iters) <= 1
+    scale = max(np.abs(r).max() for r in ref)
+    assert max(np.abs(x - r).max() for x, r in zip(xs, ref)) / scale < 1e-8
+
+
+def test_amr_polycrystal_mixed_error():
+    Ls, Cs, bc, bs = polycrystal_amr(16, 2)
+    ref, st, rc = po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, [np.zeros_like(b) for b in bs], bs, 1e-11, 0.0)
+    xs, stats = gpu_amr_solve(Ls, models.MAJORMINOR, Cs, bc, bs, precision="mixed")
+    assert stats.converged and stats.resfinal <= stats.target
+    scale = max(np.abs(r).max() for r in ref)
+    assert max(np.abs(x - r).max() for x, r in zip(xs, ref)) / scale < 1e-7
+
+
+def test_amr_trig_known_answer_on_gpu():
+    n, nlev = 32, 2
+    Ls = po.amr_levels(n, nlev)
+    bct = np.zeros((26, 3), np.int32)
+    bs, Cs, ex = [], [], []
+    for L in Ls:
+        X, Y, Z = po.node_coords(L)
+        S3 = np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+        b = np.zeros((3,) + L.shape)
+        b[0] = S3
+        bs.append(b)
+        Cs.append(np.ones((9,) + L.shape))
+        ex.append(-S3 / (3 * np.pi ** 2))
+    from anisotropicfracture_gb300.elastic import BCElastic
+    xs, stats = gpu_amr_solve(Ls, models.DIAGONAL, Cs, BCElastic(), bs, fmg=100000000, bottom=1, nu=2)
+    assert stats.converged
+    err = 0.0
+    for a, L in enumerate(Ls):
+        g = L.ng
+        sl = (slice(g, -g),) * 3 if g else (slice(None),) * 3
+        err = max(err, np.abs(xs[a][0][sl] - ex[a][sl]).max())
+    assert err / np.abs(ex[0]).max() < 0.02

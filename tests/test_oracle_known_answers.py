@@ -311,3 +311,55 @@ def test_transfer_operators_exactness():
     Zf, Yf, Xf = np.meshgrid(xf, xf, xf, indexing="ij")
     linf = 1.0 + 2 * Xf - Yf + 0.5 * Zf + 0.25 * Xf * Yf * Zf
     assert np.allclose(fine[0], linf, atol=1e-13) and np.allclose(fine[1], 2 * linf, atol=1e-13)
+
+
+# ---------------------------------------------------------------- multi-level (src/test.cc:123-151)
+def _amr_trig(nlev, n=32):
+    Ls = po.amr_levels(n, nlev)
+    bct, bcv = np.zeros((26, 3), np.int32), np.zeros((26, 3))
+    bs, us, Cs, ex = [], [], [], []
+    for L in Ls:
+        X, Y, Z = po.node_coords(L)
+        S3 = np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+        b = np.zeros((3,) + L.shape)
+        b[0] = S3
+        bs.append(po.bc_init(L, bct, bcv, b))
+        us.append(np.zeros_like(b))
+        Cs.append(np.ones((9,) + L.shape))
+        ex.append(-S3 / (3 * np.pi ** 2))
+    return Ls, bct, bs, us, Cs, ex
+
+
+def _valid(a, L):
+    g = L.ng
+    return a[(slice(None),) + (slice(g, a.shape[1] - g),) * 3] if g else a
+
+
+@pytest.mark.parametrize("nlev", [2, 3])
+def test_trig_solve_multilevel(nlev):
+    """TrigTest on 2 and 3 AMR levels (each refining the central half): composite solve within 2 %."""
+    Ls, bct, bs, us, Cs, ex = _amr_trig(nlev)
+    u, st, rc = po.solve_amr(Ls, po.ORC_DIAGONAL, Cs, bct, us, bs, 1e-8, 1e-8, max_fmg_iter=0, bottom=0)
+    assert rc == 0
+    err = max(np.abs(_valid(u[a], L)[0] - _valid(ex[a][None], L)[0]).max() for a, L in enumerate(Ls))
+    assert err / np.abs(ex[0]).max() < 0.02
+
+
+@pytest.mark.parametrize("nlev", [2, 3])
+def test_uniaxial_solve_multilevel(nlev):
+    """UniaxialTest on 2 and 3 AMR levels within 1 %."""
+    Ls = po.amr_levels(32, nlev)
+    bc = bc_uniaxial_x()
+    bs, us, Cs, ex = [], [], [], []
+    for L in Ls:
+        X, Y, Z = po.node_coords(L)
+        c = np.empty((2,) + L.shape)
+        c[0], c[1] = 6.0, 2.6
+        bs.append(po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)))
+        us.append(np.zeros((3,) + L.shape))
+        Cs.append(c)
+        ex.append(0.1 * X)
+    u, st, rc = po.solve_amr(Ls, po.ORC_ISOTROPIC, Cs, bc.type, us, bs, 1e-8, 1e-8)
+    assert rc == 0
+    err = max(np.abs(_valid(u[a], L)[0] - _valid(ex[a][None], L)[0]).max() for a, L in enumerate(Ls))
+    assert err / 0.1 < 0.01
