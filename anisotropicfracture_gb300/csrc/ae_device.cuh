@@ -231,6 +231,79 @@ __device__ __forceinline__ void gradC_col(const R* __restrict__ C, long long cs,
 #undef DC
 }
 
+// Column d of (dC : grad u) with the slot differences supplied by a callable dC(q); the same
+// 15-of-21 slot selection as gradC_col.
+template <int M, class R, class F>
+__device__ __forceinline__ void gradC_col_f(F&& dC, const R g[3][3], int d, R col[3]) {
+    if (M == MM) {
+        const R e00 = g[0][0], e11 = g[1][1], e22 = g[2][2];
+        const R e01 = g[0][1] + g[1][0], e02 = g[0][2] + g[2][0], e12 = g[1][2] + g[2][1];
+        if (d == 0) {
+            const R a0 = dC(0), a1 = dC(1), a2 = dC(2), a3 = dC(3), a4 = dC(4), a5 = dC(5), a6 = dC(6), a7 = dC(7);
+            const R a8 = dC(8), a9 = dC(9), a10 = dC(10), a11 = dC(11), a12 = dC(12), a13 = dC(13), a14 = dC(14);
+            col[0] = a0 * e00 + a1 * e01 + a2 * e02 + a3 * e11 + a4 * e12 + a5 * e22;
+            col[1] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
+            col[2] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
+        } else if (d == 1) {
+            const R a1 = dC(1), a3 = dC(3), a4 = dC(4), a6 = dC(6), a7 = dC(7), a8 = dC(8), a9 = dC(9), a10 = dC(10);
+            const R a12 = dC(12), a13 = dC(13), a15 = dC(15), a16 = dC(16), a17 = dC(17), a18 = dC(18), a19 = dC(19);
+            col[0] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
+            col[1] = a3 * e00 + a8 * e01 + a12 * e02 + a15 * e11 + a16 * e12 + a17 * e22;
+            col[2] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
+        } else {
+            const R a2 = dC(2), a4 = dC(4), a5 = dC(5), a7 = dC(7), a9 = dC(9), a10 = dC(10), a11 = dC(11), a12 = dC(12);
+            const R a13 = dC(13), a14 = dC(14), a16 = dC(16), a17 = dC(17), a18 = dC(18), a19 = dC(19), a20 = dC(20);
+            col[0] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
+            col[1] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
+            col[2] = a5 * e00 + a10 * e01 + a14 * e02 + a17 * e11 + a19 * e12 + a20 * e22;
+        }
+    } else if (M == ISO) {
+        const R dl = dC(0), dm = dC(1);
+        const R tr = dl * (g[0][0] + g[1][1] + g[2][2]);
+        if (d == 0) {
+            col[0] = tr + R(2) * dm * g[0][0];
+            col[1] = dm * (g[0][1] + g[1][0]);
+            col[2] = dm * (g[2][0] + g[0][2]);
+        } else if (d == 1) {
+            col[0] = dm * (g[0][1] + g[1][0]);
+            col[1] = tr + R(2) * dm * g[1][1];
+            col[2] = dm * (g[1][2] + g[2][1]);
+        } else {
+            col[0] = dm * (g[2][0] + g[0][2]);
+            col[1] = dm * (g[1][2] + g[2][1]);
+            col[2] = tr + R(2) * dm * g[2][2];
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) col[r] = dC(3 * r + d) * g[r][d];
+    }
+}
+
+// Slots that the z column of the grad C term reads (gradC_col, d = 2), in order.
+template <int M> struct ZSlots;
+template <> struct ZSlots<MM> {
+    static constexpr int n = 15;
+    __device__ static constexpr int at(int s) {
+        return s < 1 ? 2 : s < 2 ? 4 : s < 3 ? 5 : s < 4 ? 7 : s < 5 ? 9 : s < 6 ? 10 : s < 7 ? 11 : s < 8 ? 12
+             : s < 9 ? 13 : s < 10 ? 14 : s < 11 ? 16 : s < 12 ? 17 : s < 13 ? 18 : s < 14 ? 19 : 20;
+    }
+};
+template <> struct ZSlots<ISO> {
+    static constexpr int n = 2;
+    __device__ static constexpr int at(int s) { return s; }
+};
+template <> struct ZSlots<DIAG> {
+    static constexpr int n = 3;
+    __device__ static constexpr int at(int s) { return 3 * s + 2; }
+};
+// position of slot q in the ZSlots list (-1 if absent)
+template <int M>
+__device__ __forceinline__ constexpr int zslot_index(int q) {
+    for (int s = 0; s < ZSlots<M>::n; ++s)
+        if (ZSlots<M>::at(s) == q) return s;
+    return -1;
+}
+
 // ------------------------------------------------------------------ the operator at one node
 // f = A u at node (i,j,k): boundary rows through the BC table, interior rows
 // C : grad grad u + sum_d (d_d C : grad u) e_d  (src/Operator/Elastic.cpp:174-258).

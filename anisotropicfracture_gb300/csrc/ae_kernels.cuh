@@ -149,10 +149,226 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg r
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
         const R xv = xi.p[ox + n * xi.sc];
-        const R dx = xv * D.p[od + n * D.sc];
-        const R rx = v[n] - dx;
-        xo.p[oo + n * xo.sc] = (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
+        if (sizeof(R) == 8) {
+            // the reference's update, (1-w) x + w (b - (Ax - D x)) / D (Operator.cpp:154)
+            const R dx = xv * D.p[od + n * D.sc];
+            const R rx = v[n] - dx;
+            xo.p[oo + n * xo.sc] =
+                (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
+        } else {
+            // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D
+            xo.p[oo + n * xo.sc] = xv + omega * (b.p[ob + n * b.sc] - v[n]) * invD.p[od + n * invD.sc];
+        }
     }
+}
+
+// ------------------------------------------------------------------ z-marching tiled stencil sweeps
+// A block owns a TX x TY column of nodes and marches KZ planes in z.  Displacement planes and
+// stiffness planes sit in shared-memory rings with a one-node halo in x and y, filled by
+// asynchronous global->shared copies (cp.async) one plane ahead of the plane being computed,
+// so HBM streams while the block computes.  The stiffness slots the z column of the grad C
+// term needs at k-1 are kept in registers.  Every array element is read from global memory
+// once per block (plus the halo), all reads coalesced along i.  Domain-boundary nodes (a thin
+// shell) take the per-node path.  The views must be the level's internal storage views (halo
+// copies are guarded by the storage box).
+enum SweepOp { OP_FAPPLY = 0, OP_JACOBI = 1, OP_RESIDUAL = 2 };
+constexpr int TX = 32, TY = 8, KZ = 32;
+constexpr int HX = TX + 2, HY = TY + 2, HP = HX * HY;
+constexpr int NU_SLOTS = 4, NC_SLOTS = 3;  // displacement planes k-1..k+2, stiffness planes k..k+2
+
+template <int M, class R>
+constexpr size_t tiled_smem_bytes() {
+    return sizeof(R) * (size_t)(NU_SLOTS * 3 + NC_SLOTS * NCoef<M>::value) * HP;
+}
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gsrc), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int M, class R, int OP>
+__global__ void __launch_bounds__(TX* TY, 2) k_tiled(OpParams P, SCoef<R> K, Box3 box, View<const R> C,
+                                                     View<const R> x, View<const R> b, View<const R> invD,
+                                                     View<const R> D, View<R> out, R omega) {
+    constexpr int NC = NCoef<M>::value;
+    constexpr int NZ = ZSlots<M>::n;
+    constexpr int NT = TX * TY;
+    static_assert(NT < HP && HP <= 2 * NT, "each thread stages two halo positions per plane");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    R* su = reinterpret_cast<R*>(smraw);  // [NU_SLOTS][3 comps][HP]
+    R* sC = su + NU_SLOTS * 3 * HP;        // [NC_SLOTS][NC][HP]
+    const Geo& g = P.g;
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int i0 = box.lo[0] + blockIdx.x * TX, j0 = box.lo[1] + blockIdx.y * TY;
+    const int kbeg = box.lo[2] + blockIdx.z * KZ;
+    const int kend = min(kbeg + KZ, box.hi[2] + 1);
+    const int i = i0 + tx, j = j0 + ty;
+    const bool active = i <= box.hi[0] && j <= box.hi[1];
+    int slo[3], shi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { slo[d] = g.vlo[d] - g.ng; shi[d] = g.vhi[d] + g.ng; }
+
+    // the two halo positions this thread stages in every plane, their in-plane offsets and validity
+    const int r0 = threadIdx.x, r1 = threadIdx.x + NT;
+    const bool has1 = r1 < HP;
+    auto xy_of = [&](int r, long long& ou, long long& oc, bool& ok) {
+        const int hy = r / HX, hx = r - hy * HX;
+        const int gi = i0 - 1 + hx, gj = j0 - 1 + hy;
+        ok = gi >= slo[0] && gi <= shi[0] && gj >= slo[1] && gj <= shi[1];
+        ou = (long long)(gi - x.lo[0]) + (long long)(gj - x.lo[1]) * x.sy;
+        oc = (long long)(gi - C.lo[0]) + (long long)(gj - C.lo[1]) * C.sy;
+    };
+    long long ou0, oc0, ou1 = 0, oc1 = 0;
+    bool ok0, ok1 = false;
+    xy_of(r0, ou0, oc0, ok0);
+    if (has1) xy_of(r1, ou1, oc1, ok1);
+    // asynchronous copy of plane kk of a field into a ring slot (zeros where the halo leaves storage)
+    auto stage = [&](const View<const R>& v, long long o0, long long o1, int ncomp, int kk, R* dst) {
+        const bool kok = kk >= slo[2] && kk <= shi[2];
+        const R* base = v.p + (long long)(kk - v.lo[2]) * v.sz;
+        for (int c = 0; c < ncomp; ++c) {
+            const R* src = base + (long long)c * v.sc;
+            if (kok && ok0) cp_async<sizeof(R)>(dst + c * HP + r0, src + o0);
+            else dst[c * HP + r0] = R(0);
+            if (has1) {
+                if (kok && ok1) cp_async<sizeof(R)>(dst + c * HP + r1, src + o1);
+                else dst[c * HP + r1] = R(0);
+            }
+        }
+    };
+    auto uslot = [&](int kk) { return su + ((kk - kbeg + 1) & 3) * 3 * HP; };
+    auto cslot = [&](int kk) { return sC + ((kk - kbeg) % NC_SLOTS) * NC * HP; };
+
+    // prologue: planes k-1..k+1 (displacement) and k, k+1 (stiffness); then the lookahead plane
+    stage(x, ou0, ou1, 3, kbeg - 1, uslot(kbeg - 1));
+    stage(x, ou0, ou1, 3, kbeg, uslot(kbeg));
+    stage(x, ou0, ou1, 3, kbeg + 1, uslot(kbeg + 1));
+    stage(C, oc0, oc1, NC, kbeg, cslot(kbeg));
+    stage(C, oc0, oc1, NC, kbeg + 1, cslot(kbeg + 1));
+    cp_async_commit();
+    stage(x, ou0, ou1, 3, kbeg + 2, uslot(kbeg + 2));
+    stage(C, oc0, oc1, NC, kbeg + 2, cslot(kbeg + 2));
+    cp_async_commit();
+    R Cm[NZ];
+    const bool km_ok = active && kbeg - 1 >= slo[2];
+#pragma unroll
+    for (int s = 0; s < NZ; ++s)
+        Cm[s] = km_ok ? __ldg(C.p + C.at(i, j, kbeg - 1) + ZSlots<M>::at(s) * C.sc) : R(0);
+    cp_async_wait<1>();
+    __syncthreads();
+
+    const int idx = (ty + 1) * HX + (tx + 1);
+    for (int k = kbeg; k < kend; ++k) {
+        const R* Uc = uslot(k);
+        const R* Um = uslot(k - 1);
+        const R* Up = uslot(k + 1);
+        const R* Cc = cslot(k);
+        const R* Cn = cslot(k + 1);
+        if (active) {
+            const long long oo = out.at(i, j, k);
+            bool done = false;
+            if (OP == OP_JACOBI) {
+                if (!in_box(g.dlo, g.dhi, i, j, k)) {
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) out.p[oo + n * out.sc] = Uc[n * HP + idx];
+                    done = true;
+                } else if (g.ng >= 2 && (i == g.vlo[0] - 2 || i == g.vhi[0] + 2 || j == g.vlo[1] - 2 ||
+                                         j == g.vhi[1] + 2 || k == g.vlo[2] - 2 || k == g.vhi[2] + 2)) {
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) out.p[oo + n * out.sc] = R(0);
+                    done = true;
+                }
+            }
+            if (!done) {
+                R f[3];
+                const bool interior = i > g.dlo[0] && i < g.dhi[0] && j > g.dlo[1] && j < g.dhi[1] &&
+                                      k > g.dlo[2] && k < g.dhi[2];
+                if (!interior) {
+                    apply_node<M, R>(g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, x.p, x.sc,
+                                     x.at(i, j, k), x.sy, x.sz, i, j, k, f);
+                } else {
+                    R gu[3][3], bb[3][3][3];
+#pragma unroll
+                    for (int p = 0; p < 3; ++p) {
+                        const R* u0 = Uc + p * HP + idx;
+                        const R* um = Um + p * HP + idx;
+                        const R* up = Up + p * HP + idx;
+                        const R c0 = u0[0];
+                        const R xm = u0[-1], xp = u0[1], ym = u0[-HX], yp = u0[HX], zm = um[0], zp = up[0];
+                        gu[p][0] = (xp - xm) * K.h[0];
+                        gu[p][1] = (yp - ym) * K.h[1];
+                        gu[p][2] = (zp - zm) * K.h[2];
+                        bb[p][0][0] = (xp - R(2) * c0 + xm) * K.i2[0];
+                        bb[p][1][1] = (yp - R(2) * c0 + ym) * K.i2[1];
+                        bb[p][2][2] = (zp - R(2) * c0 + zm) * K.i2[2];
+                        bb[p][0][1] = (u0[1 + HX] + u0[-1 - HX] - u0[1 - HX] - u0[-1 + HX]) * K.m01;
+                        bb[p][0][2] = (up[1] + um[-1] - um[1] - up[-1]) * K.m02;
+                        bb[p][1][2] = (up[HX] + um[-HX] - um[HX] - up[-HX]) * K.m12;
+                        bb[p][1][0] = bb[p][0][1];
+                        bb[p][2][0] = bb[p][0][2];
+                        bb[p][2][1] = bb[p][1][2];
+                    }
+                    R a[NC];
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) a[q] = Cc[q * HP + idx];
+                    div_of<M, R>(a, bb, f);
+                    if (!P.uniform) {
+                        R c0v[3], c1v[3], c2v[3];
+                        gradC_col_f<M, R>([&](int q) { return Cc[q * HP + idx + 1] - Cc[q * HP + idx - 1]; }, gu, 0,
+                                          c0v);
+                        gradC_col_f<M, R>([&](int q) { return Cc[q * HP + idx + HX] - Cc[q * HP + idx - HX]; }, gu, 1,
+                                          c1v);
+                        gradC_col_f<M, R>([&](int q) { return Cn[q * HP + idx] - Cm[zslot_index<M>(q)]; }, gu, 2,
+                                          c2v);
+#pragma unroll
+                        for (int r = 0; r < 3; ++r) f[r] += (c0v[r] * K.h[0] + c1v[r] * K.h[1]) + c2v[r] * K.h[2];
+                    }
+                }
+                if (OP == OP_FAPPLY) {
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) out.p[oo + n * out.sc] = f[n];
+                } else if (OP == OP_RESIDUAL) {
+                    const long long ob = b.at(i, j, k);
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) out.p[oo + n * out.sc] = b.p[ob + n * b.sc] - f[n];
+                } else {
+                    const long long ob = b.at(i, j, k), od = invD.at(i, j, k);
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) {
+                        const R xv = Uc[n * HP + idx];
+                        if (sizeof(R) == 8) {
+                            const R rx = f[n] - xv * D.p[od + n * D.sc];
+                            out.p[oo + n * out.sc] =
+                                (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
+                        } else {
+                            out.p[oo + n * out.sc] =
+                                xv + omega * (b.p[ob + n * b.sc] - f[n]) * invD.p[od + n * invD.sc];
+                        }
+                    }
+                }
+            }
+        }
+        // the stiffness of plane k becomes the k-1 plane of the next step
+#pragma unroll
+        for (int s = 0; s < NZ; ++s) Cm[s] = Cc[ZSlots<M>::at(s) * HP + idx];
+        __syncthreads();  // every thread is done with the slots of planes k-1 (displacement) and k (stiffness)
+        if (k + 1 < kend) {
+            if (k + 3 <= kend) {  // the next lookahead plane reuses those slots
+                stage(x, ou0, ou1, 3, k + 3, uslot(k + 3));
+                stage(C, oc0, oc1, NC, k + 3, cslot(k + 3));
+            }
+            cp_async_commit();
+            cp_async_wait<1>();  // plane k+2 has landed
+            __syncthreads();
+        }
+    }
+    cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------------ Diagonal

@@ -107,6 +107,13 @@ void launch_residual(const OpParams& P, View<const R> C, View<const R> x, View<c
 template <class R>
 void launch_jacobi(const OpParams& P, View<const R> C, View<const R> invD, View<const R> D, View<const R> xi,
                    View<const R> b, View<R> xo, R omega, cudaStream_t st);
+// Fapply (op 0), damped-Jacobi sweep (op 1) or residual (op 2) with the z-marching tiled
+// kernel, on the level's internal storage views only.  tiled_init must have run once.
+template <class R>
+void launch_tiled(int op, const OpParams& P, View<const R> C, View<const R> x, View<const R> b, View<const R> invD,
+                  View<const R> D, View<R> out, R omega, cudaStream_t st);
+template <class R>
+void tiled_init();
 template <class R>
 void launch_diagonal(const OpParams& P, View<const R> C, View<R> D, View<R> invD, int* nan_flag, cudaStream_t st);
 // crse = R fine on `region` of coarse nodes (default: coarse valid ∩ domain); the weights

@@ -168,3 +168,70 @@ def test_fab_with_ghosts_and_offsets():
     ref = po.fapply(L, models.MAJORMINOR, Cf, bc.type, u)
     assert normwise_err(out[:, 2:-2, 2:-2, 2:-2], ref) <= TOL64
     assert np.all(out[:, :2] == 0) and np.all(out[:, -2:] == 0)
+
+
+# ---------------------------------------------------------------- z-marching tiled kernels
+@pytest.fixture
+def tiled64(monkeypatch):
+    """Operators created inside the test run their FP64 sweeps on the tiled kernels."""
+    monkeypatch.setenv("AE_TILED64", "1")
+    yield
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("cells,bckind,uniform", [(16, "random", False), (33, "config0", False),
+                                                  ((40, 9, 20), "random", True)])
+def test_tiled64_fapply_fsmooth(tiled64, model, cells, bckind, uniform):
+    """The tiled kernel (FP64 instantiation) matches the oracle at 1e-12, including tile edges
+    (domains that are not multiples of the tile) and the z-march boundaries."""
+    rng, L, Cf, bc, op = make_case(model, cells, bckind, uniform, 300 + model)
+    u = rng.standard_normal((3,) + L.shape)
+    f = torch.zeros((3,) + L.shape, dtype=torch.float64, device="cuda")
+    op.Fapply(0, 0, Field(f), Field(dev(u)))
+    assert normwise_err(host(f), po.fapply(L, model, Cf, bc.type, u, uniform)) <= TOL64
+    b = rng.standard_normal((3,) + L.shape)
+    xd = dev(u)
+    op.Fsmooth(0, 0, Field(xd), Field(dev(b)), 2, 2.0 / 3.0)
+    Dg = po.diagonal(L, model, Cf, bc.type)
+    ref = po.fsmooth(L, model, Cf, bc.type, Dg, u, b, 2, 2.0 / 3.0, uniform)
+    assert normwise_err(host(xd), ref) <= TOL64
+
+
+@pytest.mark.parametrize("model", [models.ISOTROPIC, models.MAJORMINOR])
+def test_tiled64_fine_patch_with_ghosts(tiled64, model):
+    """Jacobi on an AMR patch with 2 ghost layers: ghost layer 1 updated, ring zeroed."""
+    rng = np.random.default_rng(77)
+    Ls = po.amr_levels(16, 2)
+    Lf = Ls[1]
+    Cs = [random_coeffs(model, L.shape, rng) for L in Ls]
+    bc = bc_random(rng)
+    descs = [level_desc(tuple(L.dom_hi), lo=tuple(L.lo), hi=tuple(L.hi), dx=tuple(L.dx)) for L in Ls]
+    op = Elastic(descs, model)
+    for a, L in enumerate(Ls):
+        op.SetModel(a, Field(Cs[a], tuple(L.lo[d] - L.ng for d in range(3))))
+    op.SetBC(bc)
+    op.SetUniform(False)
+    op.prepareForSolve()
+    lo = tuple(Lf.lo[d] - 2 for d in range(3))
+    x = rng.standard_normal((3,) + Lf.shape)
+    b = rng.standard_normal((3,) + Lf.shape)
+    xd = dev(x)
+    op.Fsmooth(1, 0, Field(xd, lo), Field(dev(b), lo), 2, 2.0 / 3.0)
+    Dg = po.diagonal(Lf, model, Cs[1], bc.type)
+    ref = po.fsmooth(Lf, model, Cs[1], bc.type, Dg, x, b, 2, 2.0 / 3.0)
+    out = host(xd)
+    assert normwise_err(out, ref) <= TOL64
+    assert np.all(out[:, 0] == 0) and np.all(out[:, -1] == 0)  # the ring zeroed by Fsmooth
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_fsmooth_fp32_tiled(model, monkeypatch):
+    monkeypatch.setenv("AE_TILED32", "1")
+    rng, L, Cf, bc, op = make_case(model, 24, "config0", False, 91)
+    x = rng.standard_normal((3,) + L.shape).astype(np.float32)
+    b = rng.standard_normal((3,) + L.shape).astype(np.float32)
+    xd = dev(x)
+    op.Fsmooth(0, 0, Field(xd), Field(dev(b)), 2, 2.0 / 3.0)
+    Dg = po.diagonal(L, model, Cf, bc.type)
+    ref = po.fsmooth(L, model, Cf, bc.type, Dg, x.astype(np.float64), b.astype(np.float64), 2, 2.0 / 3.0)
+    assert normwise_err(host(xd).astype(np.float64), ref) <= 1e-4
