@@ -75,6 +75,9 @@ SIGNATURES = {
     "ae_stress": ([P, C.c_int, FAB, FAB, C.c_int], C.c_int),
     "ae_energy": ([P, C.c_int, FAB, FAB], C.c_int),
     "ae_solve": ([P, FAB, FAB, C.c_double, C.c_double, C.POINTER(SolverOpts), C.POINTER(SolveStats)], C.c_int),
+    "ae_bottom_solve_noalloc": ([C.POINTER(LevelDesc), C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p,
+                                 C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), C.c_void_p],
+                                C.c_int),
     "ae_kernel_launches": ([], C.c_longlong),
     "ae_profile_kernel": ([P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)], C.c_int),
 }

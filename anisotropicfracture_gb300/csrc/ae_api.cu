@@ -40,6 +40,13 @@ using namespace ae;
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+void ae::set_last_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+using namespace ae;
+
 struct ApiErr : std::runtime_error {
     int code;
     ApiErr(int c, const std::string& m) : std::runtime_error(m), code(c) {}

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <string>
 
 #include "ae_device.cuh"
 
@@ -11,6 +12,8 @@ namespace ae {
 
 // kernels launched by this library (eager launches; graph replays are added by the solver)
 extern std::atomic<long long> g_kernel_launches;
+// message returned by ae_last_error() on the calling thread
+void set_last_error(const std::string& msg);
 
 inline Box3 box_grow(Box3 b, int n) {
     for (int d = 0; d < 3; ++d) { b.lo[d] -= n; b.hi[d] += n; }

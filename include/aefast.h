@@ -169,6 +169,30 @@ int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, do
 /* Device memory of the operator (bytes), for admission control. */
 long long ae_op_device_bytes(const ae_op* op);
 
+/* Bottom solve without allocation.  No counterpart in the reference.
+ * For callers that cannot allocate device memory: an application whose memory arena already
+ * owns the GPU (an AMReX code that reserved it, say), or a loop that must not enter the CUDA
+ * allocator, but that runs its own multigrid hierarchy.  It solves the coarsest level exactly
+ * as the cycle inside ae_solve does: CG or BiCGStab in one thread block; on failure the
+ * correction is zeroed and `nuf` smoother calls (2 damped-Jacobi sweeps, w = 2/3) follow.
+ * No cudaMalloc, cudaFree or allocating library call: the work space is a fixed device array
+ * inside libaefast.so, sized for AE_NOALLOC_MAX_NODES nodes (10 x 3 doubles per node, 1.2 MB),
+ * which every GPU that loads the library holds until the process exits.  Larger levels are
+ * rejected with AE_ERR_ARG.
+ *  - level: one nodal box covering its domain (lo = 0, hi = domain_cells).
+ *  - C (ncoef per node), b and x (3 per node): DEVICE arrays in the level's nodal layout
+ *    without ghosts, [comp][k][j][i].  x receives the solution; the solve starts from zero.
+ *  - bctype: host array [26][3] of ae_bc_type.  *krylov_failed (may be NULL) receives the
+ *    number of failed Krylov solves (0 or 1).
+ *  - The first call on a device looks up the work space's device address with that device
+ *    current; make that first call before any stream capture.
+ *  - Every call shares the one work space: calls that overlap on the GPU (other streams, other
+ *    host threads) race.  The call synchronizes `stream` (a cudaStream_t) before returning. */
+#define AE_NOALLOC_MAX_NODES 4913 /* 17^3 */
+int ae_bottom_solve_noalloc(const ae_level_desc* level, int model, const double* C, const int* bctype, int uniform,
+                            const double* b, double* x, int bottom, int max_iter, double reltol, int nuf,
+                            int* krylov_failed, void* stream);
+
 /* Instrumentation (no counterpart in the reference, which times with BL_PROFILE scopes).
  * ae_kernel_launches: kernels this library has launched in the process (graph replays
  * count every kernel in the graph).  ae_profile_kernel: average CUDA-event duration of
