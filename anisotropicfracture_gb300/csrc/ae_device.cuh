@@ -180,12 +180,20 @@ __device__ __forceinline__ void div_of(const R* a, const R b[3][3][3], R f[3]) {
     else div_diag(a, b, f);
 }
 
+// read-only load: through the non-coherent cache for global memory (LDG), plain otherwise
+// (stiffness staged in shared memory)
+template <bool LDG, class T>
+__device__ __forceinline__ T ldv(const T* p) {
+    if constexpr (LDG) return __ldg(p);
+    else return *p;
+}
+
 // Column d of (dC : grad u), dC the (unscaled) central difference of the stiffness in
 // direction d.  Only the slots that feed column d are read: 15 of 21 for MajorMinor.
-template <int M, class R>
+template <int M, class R, bool LDG = true>
 __device__ __forceinline__ void gradC_col(const R* __restrict__ C, long long cs, long long c, long long o,
                                           const R g[3][3], int d, R col[3]) {
-#define DC(q) (__ldg(C + (q) * cs + c + o) - __ldg(C + (q) * cs + c - o))
+#define DC(q) (ldv<LDG>(C + (q) * cs + c + o) - ldv<LDG>(C + (q) * cs + c - o))
     if (M == MM) {
         const R e00 = g[0][0], e11 = g[1][1], e22 = g[2][2];
         const R e01 = g[0][1] + g[1][0], e02 = g[0][2] + g[2][0], e12 = g[1][2] + g[2][1];
@@ -307,8 +315,9 @@ __device__ __forceinline__ constexpr int zslot_index(int q) {
 // ------------------------------------------------------------------ the operator at one node
 // f = A u at node (i,j,k): boundary rows through the BC table, interior rows
 // C : grad grad u + sum_d (d_d C : grad u) e_d  (src/Operator/Elastic.cpp:174-258).
-// u and C are read through views whose strides may differ.
-template <int M, class R>
+// u and C are read through views whose strides may differ.  LDG = false when C lives in
+// shared memory.
+template <int M, class R, bool LDG = true>
 __device__ __forceinline__ void apply_node(const Geo& g, const SCoef<R>& K, const BCP& bc, bool uniform,
                                            const R* __restrict__ C, long long cs, long long cc,
                                            long long csy, long long csz, const R* __restrict__ U,
@@ -340,7 +349,7 @@ __device__ __forceinline__ void apply_node(const Geo& g, const SCoef<R>& K, cons
         if (need_s) {
             R a[NC];
 #pragma unroll
-            for (int q = 0; q < NC; ++q) a[q] = __ldg(C + q * cs + cc);
+            for (int q = 0; q < NC; ++q) a[q] = ldv<LDG>(C + q * cs + cc);
             stress_of<M, R>(a, gu, s);
         }
 #pragma unroll
@@ -375,14 +384,14 @@ __device__ __forceinline__ void apply_node(const Geo& g, const SCoef<R>& K, cons
     {
         R a[NC];
 #pragma unroll
-        for (int q = 0; q < NC; ++q) a[q] = __ldg(C + q * cs + cc);
+        for (int q = 0; q < NC; ++q) a[q] = ldv<LDG>(C + q * cs + cc);
         div_of<M, R>(a, b, f);
     }
     if (!uniform) {
         R c0[3], c1[3], c2[3];
-        gradC_col<M, R>(C, cs, cc, 1, gu, 0, c0);
-        gradC_col<M, R>(C, cs, cc, csy, gu, 1, c1);
-        gradC_col<M, R>(C, cs, cc, csz, gu, 2, c2);
+        gradC_col<M, R, LDG>(C, cs, cc, 1, gu, 0, c0);
+        gradC_col<M, R, LDG>(C, cs, cc, csy, gu, 1, c1);
+        gradC_col<M, R, LDG>(C, cs, cc, csz, gu, 2, c2);
 #pragma unroll
         for (int r = 0; r < 3; ++r) f[r] += (c0[r] * K.h[0] + c1[r] * K.h[1]) + c2[r] * K.h[2];
     }

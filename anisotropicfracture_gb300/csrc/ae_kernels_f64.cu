@@ -145,6 +145,8 @@ void launch_energy(const OpParams& P, View<const double> C, View<const double> u
 // MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab restated; the whole
 // Krylov loop runs inside one thread block on the coarsest level (ng = 0, storage = domain).
 constexpr int kBottomThreads = 256;
+// dynamic shared memory of the shared-memory bottom variant: 48 KB less room for the static BlkRed
+constexpr size_t kBottomSmemBytes = 47 * 1024;
 
 struct BlkRed {
     double part[kBottomThreads / 32];
@@ -183,14 +185,19 @@ __device__ __forceinline__ double blk_max(double v, BlkRed& sh) {
     return r;
 }
 
-template <int M>
+// Operations of the single-CTA bottom solve.  C, D and invD are either the level's global
+// arrays or their copies in shared memory (SMEM = true: plain loads instead of __ldg).
+template <int M, bool SMEM>
 struct BottomOps {
     const BottomArgs& a;
     SCoef<double> K;
     View<const double> Cv;
+    const double* D;
+    const double* invD;
     long long sy, sz, nn;
     int nx, ny, nz;
-    __device__ BottomOps(const BottomArgs& aa) : a(aa) {
+    __device__ BottomOps(const BottomArgs& aa, const double* C, const double* D_, const double* invD_)
+        : a(aa), D(D_), invD(invD_) {
         K = aa.K;
         const Geo& g = aa.P.g;
         nx = g.vhi[0] - g.vlo[0] + 1;
@@ -199,7 +206,7 @@ struct BottomOps {
         sy = nx;
         sz = (long long)nx * ny;
         nn = sz * nz;
-        Cv.p = aa.C;
+        Cv.p = C;
         Cv.lo[0] = g.vlo[0]; Cv.lo[1] = g.vlo[1]; Cv.lo[2] = g.vlo[2];
         Cv.sy = sy; Cv.sz = sz; Cv.sc = nn;
     }
@@ -210,7 +217,7 @@ struct BottomOps {
             const int k = (int)(t / sz), rem = (int)(t - (long long)k * sz);
             const int j = rem / nx, i = rem - j * nx;
             double v[3];
-            apply_node<M, double>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz, i + g.vlo[0],
+            apply_node<M, double, !SMEM>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz, i + g.vlo[0],
                                   j + g.vlo[1], k + g.vlo[2], v);
             out[t] = v[0];
             out[t + nn] = v[1];
@@ -234,22 +241,46 @@ struct BottomOps {
             apply(x, tmp);
             for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
                 const double xv = x[t];
-                const double rx = tmp[t] - xv * a.D[t];
-                x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * a.invD[t];
+                const double rx = tmp[t] - xv * D[t];
+                x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * invD[t];
             }
             __syncthreads();
         }
     }
 };
 
-template <int M>
+// SMEM = true: the whole level (C, D, invD, b, x and the 8 work vectors, bottom_smem_doubles)
+// lives in dynamic shared memory; x is copied back at the end.
+template <int M, bool SMEM>
 __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
     __shared__ BlkRed sh;
-    const BottomOps<M> ops(a);
-    const long long N = 3 * ops.nn;
+    extern __shared__ double smem[];
+    constexpr int NC = NCoef<M>::value;
+    const long long N = 3 * a.nn;
+    const double* Cp = a.C;
+    const double* Dp = a.D;
+    const double* invDp = a.invD;
     double* x = a.x;
     const double* b = a.b;
     double* r = a.work;
+    if (SMEM) {
+        double* sC = smem;
+        double* sD = sC + NC * a.nn;
+        double* sI = sD + N;
+        double* sb = sI + N;
+        double* sx = sb + N;
+        for (long long t = threadIdx.x; t < NC * a.nn; t += blockDim.x) sC[t] = a.C[t];
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            sD[t] = a.D[t];
+            sI[t] = a.invD[t];
+            sb[t] = a.b[t];
+            sx[t] = a.x[t];
+        }
+        __syncthreads();
+        Cp = sC; Dp = sD; invDp = sI; b = sb; x = sx;
+        r = sx + N;
+    }
+    const BottomOps<M, SMEM> ops(a, Cp, Dp, invDp);
     double* p = r + N;
     double* q = p + N;
     double* rh = q + N;
@@ -331,10 +362,23 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
         if (threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
         for (int s = 0; s < a.nuf; ++s) ops.smooth(x, b, tmp);
     }
+    if (SMEM) {
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
+    }
 }
 
+// doubles of dynamic shared memory the SMEM variant needs for nn nodes
+__host__ __device__ constexpr long long bottom_smem_doubles(int nc, long long nn) { return (nc + 36) * nn; }
+
+// Levels whose arrays fit the default 48 KB of dynamic shared memory (no function attribute,
+// so the launch is legal inside stream capture) run from shared memory; larger ones from global.
 void launch_bottom(const BottomArgs& a, cudaStream_t st) {
-    dispatch_model<double>(a.P.model, [&](auto m) { k_bottom<decltype(m)::value><<<1, kBottomThreads, 0, st>>>(a); });
+    dispatch_model<double>(a.P.model, [&](auto m) {
+        constexpr int Mv = decltype(m)::value;
+        const size_t bytes = (size_t)bottom_smem_doubles(NCoef<Mv>::value, a.nn) * sizeof(double);
+        if (bytes <= kBottomSmemBytes) k_bottom<Mv, true><<<1, kBottomThreads, bytes, st>>>(a);
+        else k_bottom<Mv, false><<<1, kBottomThreads, 0, st>>>(a);
+    });
     launched();
 }
 
