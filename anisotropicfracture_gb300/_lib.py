@@ -44,9 +44,36 @@ class SolveStats(C.Structure):
                 ("target", C.c_double), ("seconds", C.c_double)]
 
 
+class CellDesc(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("nrhs", C.c_int), ("length", C.c_double * 3)]
+
+
+class CellStats(C.Structure):
+    _fields_ = [("iters", C.c_int), ("converged", C.c_int), ("nlevels", C.c_int), ("bottom_fail", C.c_int),
+                ("res0", C.c_double), ("resfinal", C.c_double), ("target", C.c_double), ("seconds", C.c_double),
+                ("body_force", C.c_double * 3), ("mean_stress", C.c_double * 9)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_longlong), ("max_live_solves", C.c_int), ("keep_solution", C.c_int),
+                ("tol_rel", C.c_double), ("tol_abs", C.c_double), ("solver", SolverOpts)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("nrhs", C.c_int), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("latency", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("queued", C.c_longlong), ("iterations", C.c_longlong), ("hbm_used", C.c_longlong),
+                ("hbm_budget", C.c_longlong), ("busy_seconds", C.c_double), ("uptime_seconds", C.c_double)]
+
+
 # (name, argtypes) of every exported entry point; include/aefast.h declares the same set
 P = C.c_void_p
 FAB = C.POINTER(Fab)
+DP = C.POINTER(C.c_double)
 SIGNATURES = {
     "ae_last_error": ([], C.c_char_p),
     "ae_version": ([], C.c_char_p),
@@ -80,6 +107,29 @@ SIGNATURES = {
                                 C.c_int),
     "ae_kernel_launches": ([], C.c_longlong),
     "ae_profile_kernel": ([P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "ae_batch_plan_bytes": ([C.POINTER(CellDesc), C.c_int], C.c_longlong),
+    "ae_batch_create": ([C.POINTER(CellDesc), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+    "ae_batch_destroy": ([P], C.c_int),
+    "ae_batch_num_solves": ([P], C.c_int),
+    "ae_batch_num_levels": ([P, C.c_int], C.c_int),
+    "ae_batch_device_bytes": ([P], C.c_longlong),
+    "ae_batch_set_model": ([P, C.c_int, FAB], C.c_int),
+    "ae_batch_set_model_grains": ([P, C.c_int, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "ae_batch_set_load": ([P, C.c_int, DP], C.c_int),
+    "ae_batch_prepare": ([P], C.c_int),
+    "ae_batch_solve": ([P, C.c_double, C.c_double, C.POINTER(SolverOpts), C.POINTER(CellStats)], C.c_int),
+    "ae_batch_solution": ([P, C.c_int, FAB], C.c_int),
+    "ae_batch_set_shape": ([P, C.c_int, C.c_int, C.c_int], C.c_int),
+    "ae_batch_get_shape": ([P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+    "ae_server_default_opts": ([C.POINTER(ServerOpts)], None),
+    "ae_server_create": ([C.c_int, C.POINTER(ServerOpts), C.POINTER(C.c_void_p)], C.c_int),
+    "ae_server_destroy": ([P], C.c_int),
+    "ae_server_submit": ([P, C.POINTER(CellDesc), C.c_int, C.c_void_p, C.c_void_p, FAB, DP,
+                          C.POINTER(C.c_longlong)], C.c_int),
+    "ae_server_poll": ([P, C.c_longlong, C.POINTER(RequestInfo), C.POINTER(CellStats), DP], C.c_int),
+    "ae_server_wait": ([P, C.c_longlong, C.c_double, C.POINTER(RequestInfo), C.POINTER(CellStats), DP], C.c_int),
+    "ae_server_release": ([P, C.c_longlong], C.c_int),
+    "ae_server_get_stats": ([P, C.POINTER(ServerStats)], C.c_int),
 }
 
 _lib = None

@@ -16,7 +16,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", CSRC, "-I", INCLUDE]
 
-SOURCES = ["ae_kernels_f64.cu", "ae_kernels_f32.cu", "ae_api.cu", "ae_noalloc.cu"]
+SOURCES = ["ae_kernels_f64.cu", "ae_kernels_f32.cu", "ae_api.cu", "ae_noalloc.cu", "ae_cells_kernels.cu",
+           "ae_cells.cu", "ae_server.cu"]
 
 
 def _deps():
@@ -43,7 +44,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     tmp = LIB + ".tmp.%d" % os.getpid()
-    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

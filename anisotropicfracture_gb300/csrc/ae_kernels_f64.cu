@@ -3,6 +3,7 @@
 #include <type_traits>
 
 #include "ae_kernels.cuh"
+#include "ae_krylov.cuh"
 
 #define AE_REAL double
 #include "ae_kernels_common.inc"
@@ -142,51 +143,10 @@ void launch_energy(const OpParams& P, View<const double> C, View<const double> u
 }
 
 // ------------------------------------------------------------------ bottom solve (one CTA)
-// MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab restated; the whole
+// MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab (krylov_bottom); the whole
 // Krylov loop runs inside one thread block on the coarsest level (ng = 0, storage = domain).
-constexpr int kBottomThreads = 256;
-// dynamic shared memory of the shared-memory bottom variant: 48 KB less room for the static BlkRed
-constexpr size_t kBottomSmemBytes = 47 * 1024;
-
-struct BlkRed {
-    double part[kBottomThreads / 32];
-    double res[2];
-};
-__device__ __forceinline__ double blk_sum(double v, BlkRed& sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sh.part[w] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh.part[q];
-        sh.res[0] = s;
-    }
-    __syncthreads();
-    const double r = sh.res[0];
-    __syncthreads();
-    return r;
-}
-__device__ __forceinline__ double blk_max(double v, BlkRed& sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sh.part[w] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s = fmax(s, sh.part[q]);
-        sh.res[0] = s;
-    }
-    __syncthreads();
-    const double r = sh.res[0];
-    __syncthreads();
-    return r;
-}
-
-// Operations of the single-CTA bottom solve.  C, D and invD are either the level's global
-// arrays or their copies in shared memory (SMEM = true: plain loads instead of __ldg).
+// C, D and invD are either the level's global arrays or their copies in shared memory
+// (SMEM = true: plain loads instead of __ldg).
 template <int M, bool SMEM>
 struct BottomOps {
     const BottomArgs& a;
@@ -211,18 +171,23 @@ struct BottomOps {
         Cv.sy = sy; Cv.sz = sz; Cv.sc = nn;
     }
     // out = A x over every node
-    __device__ void apply(const double* x, double* out) const {
+    __device__ void apply(const double* x, double* out, BlkRed&) const {
         const Geo& g = a.P.g;
         for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
             const int k = (int)(t / sz), rem = (int)(t - (long long)k * sz);
             const int j = rem / nx, i = rem - j * nx;
             double v[3];
-            apply_node<M, double, !SMEM>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz, i + g.vlo[0],
-                                  j + g.vlo[1], k + g.vlo[2], v);
+            apply_node<M, double, !SMEM>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz,
+                                         i + g.vlo[0], j + g.vlo[1], k + g.vlo[2], v);
             out[t] = v[0];
             out[t + nn] = v[1];
             out[t + 2 * nn] = v[2];
         }
+        __syncthreads();
+    }
+    __device__ void residual(const double* x, const double* b, double* r, BlkRed& sh) const {
+        apply(x, r, sh);
+        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) r[t] = b[t] - r[t];
         __syncthreads();
     }
     __device__ double dot(const double* x, const double* y, BlkRed& sh) const {
@@ -236,9 +201,9 @@ struct BottomOps {
         return blk_max(s, sh);
     }
     // one Fsmooth call: a.sweeps damped-Jacobi sweeps (ng = 0: every node is updated)
-    __device__ void smooth(double* x, const double* b, double* tmp) const {
+    __device__ void smooth(double* x, const double* b, double* tmp, BlkRed& sh) const {
         for (int s = 0; s < a.sweeps; ++s) {
-            apply(x, tmp);
+            apply(x, tmp, sh);
             for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
                 const double xv = x[t];
                 const double rx = tmp[t] - xv * D[t];
@@ -262,7 +227,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
     const double* invDp = a.invD;
     double* x = a.x;
     const double* b = a.b;
-    double* r = a.work;
+    double* work = a.work;
     if (SMEM) {
         double* sC = smem;
         double* sD = sC + NC * a.nn;
@@ -278,90 +243,12 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
         }
         __syncthreads();
         Cp = sC; Dp = sD; invDp = sI; b = sb; x = sx;
-        r = sx + N;
+        work = sx + N;
     }
     const BottomOps<M, SMEM> ops(a, Cp, Dp, invDp);
-    double* p = r + N;
-    double* q = p + N;
-    double* rh = q + N;
-    double* v = rh + N;
-    double* tt = v + N;
-    double* sorig = tt + N;
-    double* tmp = sorig + N;
-    const double eps_rel = a.reltol, eps_abs = -1.0;
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) sorig[t] = x[t];
-    __syncthreads();
-    ops.apply(x, tmp);
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) { r[t] = b[t] - tmp[t]; x[t] = 0.0; }
-    __syncthreads();
-    double rnorm = ops.ninf(r, sh);
-    const double rnorm0 = rnorm;
-    int ret = 0;
-    if (!(rnorm0 == 0.0 || rnorm0 < eps_abs)) {
-        if (a.bottom == 0) {
-            double rho_1 = 0.0;
-            for (int iter = 1; iter <= a.maxiter; ++iter) {
-                const double rho = ops.dot(r, r, sh);  // z = r (no preconditioner)
-                if (rho == 0.0) { ret = 1; break; }
-                const double beta = iter == 1 ? 0.0 : rho / rho_1;
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = iter == 1 ? r[t] : r[t] + beta * p[t];
-                __syncthreads();
-                ops.apply(p, q);
-                const double pw = ops.dot(p, q, sh);
-                if (pw == 0.0) { ret = 1; break; }
-                const double alpha = rho / pw;
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * q[t]; }
-                __syncthreads();
-                rnorm = ops.ninf(r, sh);
-                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-                rho_1 = rho;
-            }
-        } else {
-            double rho_1 = 0.0, alpha = 0.0, omega = 0.0;
-            for (long long t = threadIdx.x; t < N; t += blockDim.x) { rh[t] = r[t]; p[t] = 0.0; v[t] = 0.0; }
-            __syncthreads();
-            for (int iter = 1; iter <= a.maxiter; ++iter) {
-                const double rho = ops.dot(rh, r, sh);
-                if (rho == 0.0) { ret = 1; break; }
-                if (iter == 1) {
-                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t];
-                } else {
-                    const double beta = (rho / rho_1) * (alpha / omega);
-                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t] + beta * (p[t] - omega * v[t]);
-                }
-                __syncthreads();
-                ops.apply(p, v);
-                const double rhTv = ops.dot(rh, v, sh);
-                if (rhTv != 0.0) alpha = rho / rhTv;
-                else { ret = 2; break; }
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * v[t]; }
-                __syncthreads();
-                rnorm = ops.ninf(r, sh);
-                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-                ops.apply(r, tt);
-                const double t_t = ops.dot(tt, tt, sh), t_r = ops.dot(tt, r, sh);
-                if (t_t != 0.0) omega = t_r / t_t;
-                else { ret = 3; break; }
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += omega * r[t]; r[t] += -omega * tt[t]; }
-                __syncthreads();
-                rnorm = ops.ninf(r, sh);
-                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-                if (omega == 0.0) { ret = 4; break; }
-                rho_1 = rho;
-            }
-        }
-        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
-    }
-    const bool keep = (ret == 0 || ret == 8) && rnorm < rnorm0;
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = keep ? x[t] + sorig[t] : sorig[t];
-    __syncthreads();
-    // MLMG: on failure the correction is zeroed and nuf smoother calls follow
-    if (ret != 0 && ret != 9) {
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
-        __syncthreads();
-        if (threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
-        for (int s = 0; s < a.nuf; ++s) ops.smooth(x, b, tmp);
-    }
+    const KrylovParams kp{a.bottom, a.maxiter, a.reltol, a.nuf};
+    const int ret = krylov_bottom(ops, kp, N, x, b, work, sh);
+    if (ret != 0 && ret != 9 && threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
     if (SMEM) {
         for (long long t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
     }

@@ -13,6 +13,14 @@ relative residual.  One step = one full solve from u = 0 on inputs resident in H
   roofline     the FP32 fused Jacobi sweep on the finest coarse level (the dominant kernel)
   cpu_baseline the FP64 oracle (a C++ restatement of the reference's CPU path) on a bounded
                sample of the same workload, extrapolated to one solve
+  batch        batched periodic RVEs: 512 polycrystal cells, edges uniform in {16,24,32,48,64}
+               (seed 4), 8-32 grains each (seed 5 + cell), exx = 1e-3, to 1e-8; all cells in one
+               graph-replayed batch (mixed precision, and FP64) against the same solves run one
+               cell at a time in FP64; the FP64 oracle on a sample of cells as the CPU baseline
+  serve        served homogenisation: Poisson request streams (seed 6) of cells with edges
+               uniform in {32, 40, ..., 128}, 8-64 grains and the six unit strains (1e-3) as
+               load cases, into the continuous-batching server; p50/p99 latency and solves/s per
+               arrival rate, mixed against FP64
 
 python bench.py --gpus N --steps K --warmup W [--impl reference]
 """
@@ -196,6 +204,197 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- batched and served cells
+BATCH_EDGES = (16, 24, 32, 48, 64)
+SERVE_EDGES = tuple(range(32, 129, 8))
+CELL_SOLVER = dict(max_fmg_iter=0, nu1=2, nu2=2, sweeps=2, bottom=1, bottom_max_iter=200, bottom_reltol=1e-4,
+                   nuf=8, max_iter=200)
+
+
+def batch_workload(ncells=512, seed=4):
+    """Cells of the batched workload: edge, grain count, seeds and per-grain stiffness tables."""
+    from anisotropicfracture_gb300 import cells
+    rng = np.random.default_rng(seed)
+    edges = rng.choice(BATCH_EDGES, size=ncells)
+    out = []
+    for c in range(ncells):
+        g = np.random.default_rng(5 + c)
+        ngr = int(g.integers(8, 33))
+        seeds, table = cells.rve_grains(int(edges[c]), ngr, int(g.integers(1 << 30)))
+        out.append({"n": int(edges[c]), "ngrains": ngr, "seeds": seeds, "table": table})
+    return out
+
+
+def serve_workload(nreq, seed=6):
+    from anisotropicfracture_gb300 import cells
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nreq):
+        n = int(rng.choice(SERVE_EDGES))
+        ngr = int(rng.integers(8, 65))
+        seeds, table = cells.rve_grains(n, ngr, int(rng.integers(1 << 30)))
+        out.append({"n": n, "ngrains": ngr, "seeds": seeds, "table": table})
+    return out
+
+
+def _exx():
+    E = np.zeros((3, 3))
+    E[0, 0] = 1e-3
+    return E
+
+
+def make_cell_batch(work, nrhs_loads=None):
+    from anisotropicfracture_gb300 import cells, models
+    loads = [_exx()] if nrhs_loads is None else nrhs_loads
+    B = cells.CellBatch([(w["n"], len(loads)) for w in work], models.MAJORMINOR)
+    s = 0
+    for c, w in enumerate(work):
+        B.set_grains(c, w["seeds"], w["table"])
+        for E in loads:
+            B.set_load(s, E)
+            s += 1
+    B.prepare()
+    return B
+
+
+def cpu_cells_sample(work, nsample, threads=None):
+    """FP64 oracle cell solves of a sample of cells (stiffness built outside the timed region);
+    returns (seconds, nodes) of the sample."""
+    from anisotropicfracture_gb300 import cells, models
+    from oracle import pyoracle as po
+    if threads:
+        po.set_threads(threads)
+    secs, nodes = 0.0, 0
+    for w in work[:nsample]:
+        n = w["n"]
+        Cf = cells.rve_stiffness(n, w["seeds"], w["table"])
+        t0 = time.perf_counter()
+        po.rve_solve(po.rve_level(n), models.MAJORMINOR, Cf, _exx(), **CELL_SOLVER)
+        secs += time.perf_counter() - t0
+        nodes += n ** 3
+    return secs, nodes
+
+
+def bench_batch(args, lib):
+    """Batched cells: mixed and FP64 in one batch, FP64 one cell at a time, CPU oracle sample."""
+    work = batch_workload(args.batch_cells)
+    nodes = sum(w["n"] ** 3 for w in work)
+    t0 = time.perf_counter()
+    B = make_cell_batch(work)
+    setup_s = time.perf_counter() - t0
+    out = {"workload": "%d periodic polycrystal RVEs, edges uniform in %s cells (seed 4), 8-32 grains each, "
+                       "cubic 1.68/1.21/0.75, exx = 1e-3, tol_rel 1e-8" % (len(work), list(BATCH_EDGES)),
+           "cells": len(work), "nodes": nodes, "device_bytes": B.device_bytes(), "setup_s": setup_s,
+           "cycle": "V-cycle, 2 pre + 2 post smoother calls of 2 damped-Jacobi sweeps, BiCGStab bottom",
+           "inner_cycles": args.batch_inner, "unit": UNIT}
+    res = {}
+    sols = {}
+    for prec, name in ((1, "mixed"), (0, "fp64_batched")):
+        st, rc = B.solve(precision=prec, inner_cycles=args.batch_inner, check=False, **CELL_SOLVER)  # warm/tune
+        l0 = lib.ae_kernel_launches()
+        t0 = time.perf_counter()
+        reps = max(1, args.batch_steps)
+        for _ in range(reps):
+            st, rc = B.solve(precision=prec, inner_cycles=args.batch_inner, check=False, **CELL_SOLVER)
+        secs = (time.perf_counter() - t0) / reps
+        launches = (lib.ae_kernel_launches() - l0) // reps
+        res[name] = {"value": len(work) / secs, "s_per_batch": secs, "converged": rc == 0,
+                     "max_iters": max(s["iters"] for s in st), "mean_iters": float(np.mean([s["iters"] for s in st])),
+                     "gpu_launches": int(launches)}
+        sols[name] = [B.solution(s) for s in range(len(work))]
+    shapes = [B.get_shape(m) for m in range(6)]
+    B.close()
+    # the same solves one cell at a time in FP64 (set-up outside the timed region)
+    lim = len(work) if args.batch_single_limit <= 0 else min(len(work), args.batch_single_limit)
+    singles = [make_cell_batch([w]) for w in work[:lim]]
+    for Bs in singles[:2]:
+        Bs.solve(precision=0, check=False, **CELL_SOLVER)
+    t0 = time.perf_counter()
+    ok = True
+    for Bs in singles:
+        st, rc = Bs.solve(precision=0, check=False, **CELL_SOLVER)
+        ok = ok and rc == 0
+    secs = time.perf_counter() - t0
+    w64 = [Bs.solution(0) for Bs in singles]
+    for Bs in singles:
+        Bs.close()
+    res["fp64_one_at_a_time"] = {"value": lim / secs, "cells_timed": lim, "seconds": secs, "converged": ok}
+    err = 0.0
+    for a, b in zip(sols["mixed"][:lim], w64):
+        err = max(err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+    err_b = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+                for a, b in zip(sols["fp64_batched"][:lim], w64))
+    out.update(res)
+    out["mixed_over_fp64_one_at_a_time"] = res["mixed"]["value"] / res["fp64_one_at_a_time"]["value"]
+    out["mixed_over_fp64_batched"] = res["mixed"]["value"] / res["fp64_batched"]["value"]
+    out["displacement_err_mixed_vs_fp64"] = err
+    out["fp64_batched_vs_one_at_a_time"] = err_b
+    out["shapes"] = shapes
+    if not args.no_cpu:
+        try:
+            ns = max(1, args.batch_cpu_sample)
+            secs, nn = cpu_cells_sample(work, ns, threads=os.cpu_count())
+            per_node = secs / nn
+            out["cpu_baseline"] = {"value": 1.0 / (per_node * nodes / len(work)), "unit": UNIT,
+                                   "cores": os.cpu_count(), "kind": "port",
+                                   "sample": "FP64 oracle cell solves of the first %d cells (%d nodes, %.1f s), "
+                                             "scaled per node to the mean cell" % (ns, nn, secs)}
+        except Exception as e:  # pragma: no cover
+            out["cpu_baseline"] = {"value": None, "sample": "failed: %s" % e}
+    return out
+
+
+def serve_run(work, rate, precision, inner, seed=7):
+    """Poisson arrivals at `rate` requests/s into a fresh server."""
+    from anisotropicfracture_gb300 import cells, models
+    S = cells.CellServer(models.MAJORMINOR, precision=precision, inner_cycles=inner, **CELL_SOLVER)
+    loads = cells.unit_strains()
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, size=len(work))
+    tickets = []
+
+    def producer():
+        t_next = time.perf_counter()
+        for w, g in zip(work, gaps):
+            t_next += g
+            dt = t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(S.submit(w["n"], loads, w["seeds"], w["table"]))
+
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    res = [S.wait(t, 3600.0) for t in tickets]
+    st = S.stats()
+    S.close()
+    lat = np.array([r["latency"] for r in res])
+    good = [r for r in res if r["status"] == 0]
+    first = min(r["t_submit"] for r in res)
+    last = max(r["t_done"] for r in res)
+    nsolves = sum(len(r["stats"]) for r in good)
+    return {"rate": rate, "requests": len(work), "ok": len(good) == len(res), "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "solves_per_s": nsolves / (last - first),
+            "iterations": st["iterations"], "busy_s": st["busy_seconds"]}
+
+
+def bench_serve(args):
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    work = serve_workload(args.serve_requests)
+    out = {"workload": "Poisson streams (seed 6) of periodic polycrystal cells, edges uniform in {32..128 step 8}, "
+                       "8-64 grains, 6 unit strains (1e-3) per request, tol_rel 1e-8",
+           "requests_per_rate": len(work), "mean_nodes": float(np.mean([w["n"] ** 3 for w in work])),
+           "inner_cycles": args.batch_inner, "unit": UNIT}
+    # warm-up: one small request (library load, first graph capture)
+    serve_run(work[:1], 1000.0, 1, args.batch_inner)
+    for prec, name in ((1, "mixed"), (0, "fp64")):
+        runs = [serve_run(work, r, prec, args.batch_inner) for r in rates]
+        out[name] = runs
+    peak_m = max(r["solves_per_s"] for r in out["mixed"])
+    peak_f = max(r["solves_per_s"] for r in out["fp64"])
+    out["mixed_over_fp64"] = peak_m / peak_f
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -210,6 +409,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--inner", type=int, default=int(os.environ.get("AE_INNER_CYCLES", "8")),
                     help="FP32 cycles per FP64 residual in mixed precision")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-cell workload")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-cell workload")
+    ap.add_argument("--only-cells", action="store_true", help="run only the batched/served cell workloads")
+    ap.add_argument("--batch-cells", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-inner", type=int, default=2)
+    ap.add_argument("--batch-single-limit", type=int, default=0, help="cells timed one at a time (0: all)")
+    ap.add_argument("--batch-cpu-sample", type=int, default=4)
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rates", default="50,200,2000")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -217,6 +426,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.only_cells:
+        main_cells_only(args)
         return
 
     import torch
@@ -381,11 +593,40 @@ def main():
         "gpu_launches": int(launches),
         "cpu_baseline": cpu,
     }
+    op.close()
+    add_cell_workloads(args, lib, line, rank, world)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    op.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def add_cell_workloads(args, lib, line, rank, world):
+    """The batched and served cell workloads (rank 0 of a single-GPU run)."""
+    if world > 1 or rank != 0:
+        return
+    if not args.no_batch:
+        try:
+            line["batch"] = bench_batch(args, lib)
+        except Exception as e:  # pragma: no cover
+            line["batch"] = {"error": str(e)}
+    if not args.no_serve:
+        try:
+            line["serve"] = bench_serve(args)
+        except Exception as e:  # pragma: no cover
+            line["serve"] = {"error": str(e)}
+
+
+def main_cells_only(args):
+    """--only-cells: the batched and served workloads without the single-box configuration."""
+    import torch
+    from anisotropicfracture_gb300 import _lib, build as libbuild
+    torch.cuda.set_device(0)
+    libbuild.build()
+    lib = _lib.load()
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "data": "synthetic", "impl": "ours-cells"}
+    add_cell_workloads(args, lib, line, 0, 1)
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -202,6 +202,119 @@ int ae_bottom_solve_noalloc(const ae_level_desc* level, int model, const double*
 long long ae_kernel_launches(void);
 int ae_profile_kernel(ae_op* op, int which, int amrlev, int mglev, int precision, int reps, double* avg_ms);
 
+/* ---------------------------------------------------------------- periodic cells (RVEs)
+ * Homogenisation of periodic cells under a macroscopic displacement gradient E (3x3,
+ * row-major, E[3*i+j] = du_i/dx_j): u = E x + w, w periodic.  The operator is the interior row
+ * of Operator::Elastic<T>::Fapply (src/Operator/Elastic.cpp:216-255) at every node with
+ * neighbours taken modulo the cell: a periodic cell has no domain boundary, so the reference's
+ * BC::Operator::Elastic Type::Periodic rows (src/BC/Operator/Elastic.H:299-300) never occur.
+ * Because the non-divergence form is not conservative on the grid, each cell problem carries a
+ * uniform body force c: A w + c = b, mean(w) = 0, b = -sum_d (d_d C) : E e_d.  The solve is the
+ * MLMG iteration of ae_solve on the mean-free residual (V-cycles; max_fmg_iter is not used),
+ * bottom Krylov on the mean-projected operator.  No counterpart in the reference: the batched
+ * RVE solve and the serving loop below are built on its operator and cycle.
+ *
+ * A cell stores n[0] n[1] n[2] unique nodes (x = i length/n), fields [comp][k][j][i]; fabs
+ * passed for a cell have lo = 0, hi = n-1.  A batch advances every solve of every cell together:
+ * each kernel launch covers all of them and each iteration is one CUDA graph launch.  The
+ * arithmetic of one solve does not depend on the other solves of the batch. */
+typedef struct {
+    int n[3];          /* nodes (= cells) per direction */
+    int nrhs;          /* solves (load cases) on this cell */
+    double length[3];  /* cell edge lengths */
+} ae_cell_desc;
+
+typedef struct {
+    int iters, converged, nlevels, bottom_fail;
+    double res0, resfinal, target;
+    double seconds;            /* wall time of the ae_batch_solve call */
+    double body_force[3];      /* c of the last residual */
+    double mean_stress[9];     /* cell average of C : (E + grad w), central differences */
+} ae_cell_stats;
+
+typedef struct ae_batch_s* ae_batch;
+
+/* device bytes one cell needs (its hierarchy and nrhs solves), or -1 for a bad descriptor */
+long long ae_batch_plan_bytes(const ae_cell_desc* cell, int model);
+int ae_batch_create(const ae_cell_desc* cells, int ncells, int model, ae_batch* out);
+int ae_batch_destroy(ae_batch b);
+int ae_batch_num_solves(ae_batch b);  /* solves are numbered cell by cell, nrhs each */
+int ae_batch_num_levels(ae_batch b, int cell);
+long long ae_batch_device_bytes(ae_batch b);
+/* stiffness per node: a fab of ncoef FP64 components over [0, n-1]^3, host or device */
+int ae_batch_set_model(ae_batch b, int cell, const ae_fab* C);
+/* stiffness from a Voronoi cell (IC::Voronoi semantics, src/IC/Voronoi.H:47-101, with the
+ * minimum-image distance of the periodic cell; ties to the lower seed): seeds ngrains x 3 in
+ * length units, table ngrains x ncoef; host or device pointers.  Built on the device. */
+int ae_batch_set_model_grains(ae_batch b, int cell, int ngrains, const double* seeds, const double* table);
+int ae_batch_set_load(ae_batch b, int solve, const double* E);
+/* coarsened stiffness, diagonals and FP32 copies of every cell (Operator::prepareForSolve) */
+int ae_batch_prepare(ae_batch b);
+/* Solve every load case to ||r|| <= max(tol_abs, tol_rel max(||b||, ||r0||)).  opts->precision
+ * 0: FP64 cycles; 1: FP32 cycles (inner_cycles per FP64 residual) inside FP64 refinement.
+ * stats: NULL or ae_batch_num_solves entries.  AE_ERR_NOT_CONVERGED if any solve stopped at
+ * max_iter (the stats say which). */
+int ae_batch_solve(ae_batch b, double tol_rel, double tol_abs, const ae_solver_opts* opts, ae_cell_stats* stats);
+/* w (mean removed) of one solve into a 3-component fab over [0, n-1]^3, host or device */
+int ae_batch_solution(ae_batch b, int solve, ae_fab* w);
+/* Launch shape of the stencil kernels on multigrid level `level`: nodes per block (128 or 256)
+ * and persistent grid size (0: one block per 128/256-node run).  chunk = grid = 0 returns the
+ * level to the autotuner, which times the candidates on the first solve of each precision. */
+int ae_batch_set_shape(ae_batch b, int level, int chunk, int grid);
+int ae_batch_get_shape(ae_batch b, int level, int* chunk, int* grid);
+
+/* ---------------------------------------------------------------- serving
+ * A request loop for cell homogenisation.  A worker thread owns the device work and runs
+ * continuous batching: between iterations it admits queued requests (FIFO) whose device memory
+ * fits the budget, builds their stiffness and multigrid hierarchy on the device and starts their
+ * solves; every iteration advances all live solves in the same launches; a request whose load
+ * cases have all finished is completed and its memory returned.  A request's result does not
+ * depend on the other requests on the device.  Times are seconds since ae_server_create. */
+typedef struct {
+    long long hbm_budget_bytes;  /* device memory for live requests; 0 = 80 % of free memory at creation */
+    int max_live_solves;         /* admission cap on live load cases; 0 = none */
+    int keep_solution;           /* copy every load case's w back with the result */
+    double tol_rel, tol_abs;
+    ae_solver_opts solver;       /* precision, inner_cycles, cycle counts, bottom solver, use_graph */
+} ae_server_opts;
+
+typedef struct {
+    int status;      /* AE_OK done, < 0 failed (ae_status), 1 queued, 2 running */
+    int nrhs;
+    double t_submit, t_admit, t_done;
+    double latency;  /* t_done - t_submit once finished, else -1 */
+} ae_request_info;
+
+typedef struct {
+    long long submitted, completed, failed, queued, iterations;
+    long long hbm_used, hbm_budget;
+    double busy_seconds;    /* worker time spent admitting, iterating and retiring */
+    double uptime_seconds;
+} ae_server_stats;
+
+typedef struct ae_server_s* ae_server;
+
+void ae_server_default_opts(ae_server_opts* opts);  /* mixed precision, 2 inner cycles, 1e-8, graphs */
+int ae_server_create(int model, const ae_server_opts* opts, ae_server* out);
+/* Stop the worker (finishing its current iteration) and free everything; queued and running
+ * requests are dropped. */
+int ae_server_destroy(ae_server s);
+/* Queue one cell with desc->nrhs load cases (E: nrhs x 9).  The stiffness is either a Voronoi
+ * description (ngrains > 0: seeds ngrains x 3, table ngrains x ncoef, host memory; built on the
+ * device as ae_batch_set_model_grains) or a host FP64 field C (ngrains = 0).  Inputs are copied;
+ * *ticket identifies the request. */
+int ae_server_submit(ae_server s, const ae_cell_desc* desc, int ngrains, const double* seeds, const double* table,
+                     const ae_fab* C, const double* E, long long* ticket);
+/* Current state of a request; once finished, stats (nrhs entries) and w (nrhs x 3 x nn, if
+ * keep_solution) are filled when non-NULL. */
+int ae_server_poll(ae_server s, long long ticket, ae_request_info* info, ae_cell_stats* stats, double* w);
+/* As poll, after waiting until the request finishes (timeout_s < 0: no limit). */
+int ae_server_wait(ae_server s, long long ticket, double timeout_s, ae_request_info* info, ae_cell_stats* stats,
+                   double* w);
+/* Forget a finished request. */
+int ae_server_release(ae_server s, long long ticket);
+int ae_server_get_stats(ae_server s, ae_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1053,3 +1053,543 @@ int orc_solve(const orc_level* L0, int model, const double* C, const int* bctype
 }
 
 }  // extern "C"
+
+// ================================================================ periodic RVE cells
+// Homogenisation of a periodic cell under a macroscopic displacement gradient E:
+// u = E x + w with w periodic.  The operator is the interior row of Elastic<T>::Fapply
+// (src/Operator/Elastic.cpp:216-255) at every node, neighbours taken modulo the cell, since a
+// periodic cell has no domain boundary.  (The reference's BC::Operator::Elastic marks a periodic
+// face with Type::Periodic, src/BC/Operator/Elastic.H:299-300, and leaves the node coupling to
+// AMReX's periodic ghost fill.)  Because the stencils are exact on affine fields,
+// A(E x) = sum_d (d_d C) : E e_d, so w solves A w = b with b = -sum_d (d_d C) : E e_d.
+//
+// A annihilates constants but the non-divergence form is not conservative on the grid: its
+// left null vectors are not constant, so b is in general not in the range of A.  The cell
+// problem is therefore posed with a uniform body force c (the Lagrange multiplier of mean(w) = 0):
+//     A w + c = b,   mean(w) = 0,
+// which is consistent and has a unique solution.  Each MLMG-style iteration removes the mean of
+// the residual (that mean is the current c), the convergence test is on the mean-free residual,
+// and the coarsest level solves the same bordered problem with the Krylov iteration run on the
+// mean-projected operator.  Every node stores n[0] n[1] n[2] unique nodes, no ghosts, index order
+// [comp][k][j][i].
+namespace {
+
+struct PLev {
+    int n[3];
+    double dx[3];
+    long nn;
+    explicit PLev(const orc_rve_level& L) {
+        for (int d = 0; d < 3; ++d) { n[d] = L.n[d]; dx[d] = L.dx[d]; }
+        nn = (long)n[0] * n[1] * n[2];
+    }
+    long at(int i, int j, int k) const {
+        i = (i % n[0] + n[0]) % n[0];
+        j = (j % n[1] + n[1]) % n[1];
+        k = (k % n[2] + n[2]) % n[2];
+        return (long)i + (long)n[0] * (j + (long)n[1] * k);
+    }
+};
+
+template <class F>
+void for_cell(const PLev& L, F&& fn) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < L.n[2]; ++k)
+        for (int j = 0; j < L.n[1]; ++j)
+            for (int i = 0; i < L.n[0]; ++i) fn(i, j, k);
+}
+
+// value of component array f at (i,j,k) + offsets, periodic
+struct PAt {
+    const PLev& L;
+    const double* f;
+    int i, j, k;
+    double operator()(int a, int b, int c) const { return f[L.at(i + a, j + b, k + c)]; }
+};
+
+// gradient (central) and second derivatives of component p at a node, the Numeric::Stencil
+// interior formulas (src/Numeric/Stencil.H:44-176) on periodic neighbours
+inline void pgrad(const PLev& L, const double* U, int i, int j, int k, double g[3][3], double b[3][3][3]) {
+    for (int p = 0; p < 3; ++p) {
+        const PAt f{L, U + p * L.nn, i, j, k};
+        const double c0 = f(0, 0, 0);
+        g[p][0] = (f(1, 0, 0) - f(-1, 0, 0)) * 0.5 / L.dx[0];
+        g[p][1] = (f(0, 1, 0) - f(0, -1, 0)) * 0.5 / L.dx[1];
+        g[p][2] = (f(0, 0, 1) - f(0, 0, -1)) * 0.5 / L.dx[2];
+        if (!b) continue;
+        b[p][0][0] = (f(1, 0, 0) - 2.0 * c0 + f(-1, 0, 0)) / L.dx[0] / L.dx[0];
+        b[p][1][1] = (f(0, 1, 0) - 2.0 * c0 + f(0, -1, 0)) / L.dx[1] / L.dx[1];
+        b[p][2][2] = (f(0, 0, 1) - 2.0 * c0 + f(0, 0, -1)) / L.dx[2] / L.dx[2];
+        b[p][0][1] = 0.25 * (f(1, 1, 0) + f(-1, -1, 0) - f(1, -1, 0) - f(-1, 1, 0)) / (L.dx[0] * L.dx[1]);
+        b[p][0][2] = 0.25 * (f(1, 0, 1) + f(-1, 0, -1) - f(1, 0, -1) - f(-1, 0, 1)) / (L.dx[0] * L.dx[2]);
+        b[p][1][2] = 0.25 * (f(0, 1, 1) + f(0, -1, -1) - f(0, 1, -1) - f(0, -1, 1)) / (L.dx[1] * L.dx[2]);
+        b[p][1][0] = b[p][0][1];
+        b[p][2][0] = b[p][0][2];
+        b[p][2][1] = b[p][1][2];
+    }
+}
+
+// sum_d column d of (d_d C) : g  (Elastic.cpp:249-254 with central differences)
+inline void pgradC(const PLev& L, int model, const double* C, int i, int j, int k, const double g[3][3],
+                   double out[3]) {
+    const int nc = ncoef_of(model);
+    double col[3][3];
+    for (int d = 0; d < 3; ++d) {
+        const int o[3] = {d == 0, d == 1, d == 2};
+        double cg[21];
+        for (int q = 0; q < nc; ++q) {
+            const PAt c{L, C + q * L.nn, i, j, k};
+            cg[q] = (c(o[0], o[1], o[2]) - c(-o[0], -o[1], -o[2])) * 0.5 / L.dx[d];
+        }
+        double sd[3][3];
+        stress_of(model, cg, g, sd);
+        for (int r = 0; r < 3; ++r) col[d][r] = sd[r][d];
+    }
+    for (int r = 0; r < 3; ++r) out[r] = (col[0][r] + col[1][r]) + col[2][r];
+}
+
+inline void pfapply_node(const PLev& L, int model, const double* C, int uniform, const double* U, int i, int j,
+                         int k, double f[3]) {
+    const long c = L.at(i, j, k);
+    const int nc = ncoef_of(model);
+    double a[21];
+    for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
+    double g[3][3], b[3][3][3];
+    pgrad(L, U, i, j, k, g, b);
+    div_of(model, a, b, f);
+    if (!uniform) {
+        double gc[3];
+        pgradC(L, model, C, i, j, k, g, gc);
+        for (int r = 0; r < 3; ++r) f[r] += gc[r];
+    }
+}
+
+void pfapply(const PLev& L, int model, const double* C, int uniform, const double* U, double* F) {
+    for_cell(L, [&](int i, int j, int k) {
+        double f[3];
+        pfapply_node(L, model, C, uniform, U, i, j, k, f);
+        const long c = L.at(i, j, k);
+        for (int p = 0; p < 3; ++p) F[p * L.nn + c] = f[p];
+    });
+}
+
+// Elastic<T>::Diagonal interior row (src/Operator/Elastic.cpp:320-341): the central gradient
+// of a unit spike vanishes at its own node, leaving C_{pjpj} (-2 / dx_j^2)
+void pdiagonal(const PLev& L, int model, const double* C, double* D) {
+    const int nc = ncoef_of(model);
+    for_cell(L, [&](int i, int j, int k) {
+        const long c = L.at(i, j, k);
+        double a[21];
+        for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
+        for (int p = 0; p < 3; ++p) {
+            double b[3][3][3] = {};
+            for (int d = 0; d < 3; ++d) b[p][d][d] = -2.0 / L.dx[d] / L.dx[d];
+            double f[3];
+            div_of(model, a, b, f);
+            D[p * L.nn + c] = f[p];
+        }
+    });
+}
+
+// Operator<Node>::Fsmooth update (src/Operator/Operator.cpp:128-150) at every node of the cell
+void pfsmooth(const PLev& L, int model, const double* C, int uniform, const double* D, double* X, const double* B,
+              int nsweeps, double omega) {
+    std::vector<double> Ax(3 * L.nn);
+    for (int s = 0; s < nsweeps; ++s) {
+        pfapply(L, model, C, uniform, X, Ax.data());
+#pragma omp parallel for schedule(static)
+        for (long c = 0; c < 3 * L.nn; ++c) {
+            const double Dx = X[c] * D[c];
+            const double Rx = Ax[c] - Dx;
+            X[c] = (1. - omega) * X[c] + omega * (B[c] - Rx) / D[c];
+        }
+    }
+}
+
+// per-component mean, summed in node order
+void pmean(const PLev& L, const double* v, double m[3]) {
+    for (int p = 0; p < 3; ++p) {
+        double s = 0.0;
+        for (long c = 0; c < L.nn; ++c) s += v[p * L.nn + c];
+        m[p] = s / (double)L.nn;
+    }
+}
+void psubtract(const PLev& L, double* v, const double m[3]) {
+    for (int p = 0; p < 3; ++p)
+        for (long c = 0; c < L.nn; ++c) v[p * L.nn + c] -= m[p];
+}
+double pninf(const PLev& L, const double* v) {
+    double m = 0.0;
+    for (long c = 0; c < 3 * L.nn; ++c) m = std::max(m, std::fabs(v[c]));
+    return m;
+}
+
+// r = b - A x; with project, the per-component mean of r is removed (returned in mean)
+double presidual(const PLev& L, int model, const double* C, int uniform, const double* X, const double* B, double* R,
+                 int project, double mean[3]) {
+    pfapply(L, model, C, uniform, X, R);
+    for (long c = 0; c < 3 * L.nn; ++c) R[c] = B[c] + (-1.0) * R[c];
+    double m[3] = {0, 0, 0};
+    if (project) {
+        pmean(L, R, m);
+        psubtract(L, R, m);
+    }
+    if (mean)
+        for (int p = 0; p < 3; ++p) mean[p] = m[p];
+    return pninf(L, R);
+}
+
+// nodal full weighting (the interior weights of Operator<Node>::restriction,
+// src/Operator/Operator.cpp:527-541), neighbours modulo the fine cell; coarse I <- fine 2I
+void prestrict(const PLev& Lc, const PLev& Lf, int ncomp, double* crse, const double* fine) {
+    for (int n = 0; n < ncomp; ++n) {
+        for_cell(Lc, [&](int I, int J, int K) {
+            const PAt f{Lf, fine + n * Lf.nn, 2 * I, 2 * J, 2 * K};
+            const double v =
+                (f(-1, -1, -1) + f(-1, -1, +1) + f(-1, +1, -1) + f(-1, +1, +1) + f(+1, -1, -1) + f(+1, -1, +1) +
+                 f(+1, +1, -1) + f(+1, +1, +1)) / 64.0 +
+                (f(0, -1, -1) + f(0, -1, +1) + f(0, +1, -1) + f(0, +1, +1) + f(-1, 0, -1) + f(+1, 0, -1) +
+                 f(-1, 0, +1) + f(+1, 0, +1) + f(-1, -1, 0) + f(-1, +1, 0) + f(+1, -1, 0) + f(+1, +1, 0)) / 32.0 +
+                (f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(+1, 0, 0) + f(0, +1, 0) + f(0, 0, +1)) / 16.0 +
+                f(0, 0, 0) / 8.0;
+            crse[n * Lc.nn + Lc.at(I, J, K)] = v;
+        });
+    }
+}
+
+// trilinear nodal prolongation added into fine (src/Operator/Operator.cpp:586-614), coarse
+// neighbours modulo the coarse cell
+void pinterp_add(const PLev& Lf, const PLev& Lc, int ncomp, double* fine, const double* crse) {
+    for (int n = 0; n < ncomp; ++n) {
+        for_cell(Lf, [&](int i, int j, int k) {
+            const PAt c{Lc, crse + n * Lc.nn, i / 2, j / 2, k / 2};
+            const bool ie = i % 2 == 0, je = j % 2 == 0, ke = k % 2 == 0;
+            double v;
+            if (ie && je && ke) v = c(0, 0, 0);
+            else if (je && ke) v = 0.5 * (c(0, 0, 0) + c(1, 0, 0));
+            else if (ke && ie) v = 0.5 * (c(0, 0, 0) + c(0, 1, 0));
+            else if (ie && je) v = 0.5 * (c(0, 0, 0) + c(0, 0, 1));
+            else if (ie) v = 0.25 * (c(0, 0, 0) + c(0, 1, 0) + c(0, 0, 1) + c(0, 1, 1));
+            else if (je) v = 0.25 * (c(0, 0, 0) + c(0, 0, 1) + c(1, 0, 0) + c(1, 0, 1));
+            else if (ke) v = 0.25 * (c(0, 0, 0) + c(1, 0, 0) + c(0, 1, 0) + c(1, 1, 0));
+            else
+                v = 0.125 * (c(0, 0, 0) + c(1, 0, 0) + c(0, 1, 0) + c(0, 0, 1) + c(0, 1, 1) + c(1, 0, 1) + c(1, 1, 0) +
+                             c(1, 1, 1));
+            fine[n * Lf.nn + Lf.at(i, j, k)] += v;
+        });
+    }
+}
+
+bool pcoarsenable(const orc_rve_level& L) {
+    for (int d = 0; d < 3; ++d)
+        if (L.n[d] % 2 != 0 || L.n[d] / 2 < 2) return false;
+    return true;
+}
+
+struct PMG {
+    orc_rve_level ol;
+    PLev* L = nullptr;
+    std::vector<double> C, D, res, cor, rescor, corhold;
+};
+
+// The MLMG cycle of Solver above on a periodic cell; the bottom solve works on the
+// mean-projected operator.
+struct PSolver {
+    int model, nc, uniform;
+    orc_opts o;
+    std::vector<PMG> lv;
+    int bottom_fail = 0;
+    ~PSolver() { for (auto& l : lv) delete l.L; }
+
+    void apply(int m, const double* x, double* out) { pfapply(*lv[m].L, model, lv[m].C.data(), uniform, x, out); }
+    void smooth(int m, double* x, const double* b) {
+        pfsmooth(*lv[m].L, model, lv[m].C.data(), uniform, lv[m].D.data(), x, b, o.sweeps, o.omega);
+    }
+    void res_of_cor(int m) {
+        presidual(*lv[m].L, model, lv[m].C.data(), uniform, lv[m].cor.data(), lv[m].res.data(), lv[m].rescor.data(), 0,
+                  nullptr);
+    }
+    double dot(int m, const double* a, const double* b) {
+        double s = 0;
+        for (long i = 0; i < 3 * lv[m].L->nn; ++i) s += a[i] * b[i];
+        return s;
+    }
+    // A x with its per-component mean removed
+    void papply(int m, const double* x, double* out) {
+        apply(m, x, out);
+        double mu[3];
+        pmean(*lv[m].L, out, mu);
+        psubtract(*lv[m].L, out, mu);
+    }
+    // MLCGSolver CG / BiCGStab (as Solver::bottom_krylov) on P A, P the mean projection
+    int bottom_krylov(int m, double* sol, const double* rhs) {
+        const PLev& L = *lv[m].L;
+        const long N = 3 * L.nn;
+        const double eps_rel = o.bottom_reltol, eps_abs = -1.0;
+        std::vector<double> sorig(sol, sol + N), r(N);
+        double mu[3];
+        presidual(L, model, lv[m].C.data(), uniform, sol, rhs, r.data(), 1, mu);
+        std::fill(sol, sol + N, 0.0);
+        double rnorm = pninf(L, r.data());
+        const double rnorm0 = rnorm;
+        int ret = 0;
+        if (rnorm0 == 0 || rnorm0 < eps_abs) {
+            for (long i = 0; i < N; ++i) sol[i] += sorig[i];
+            return 0;
+        }
+        if (o.bottom == 0) {
+            std::vector<double> p(N, 0.0), q(N);
+            double rho_1 = 0;
+            for (int iter = 1; iter <= o.bottom_max_iter; ++iter) {
+                const double rho = dot(m, r.data(), r.data());
+                if (rho == 0) { ret = 1; break; }
+                if (iter == 1) p = r;
+                else {
+                    const double beta = rho / rho_1;
+                    for (long i = 0; i < N; ++i) p[i] = r[i] + beta * p[i];
+                }
+                papply(m, p.data(), q.data());
+                const double pw = dot(m, p.data(), q.data());
+                if (pw == 0) { ret = 1; break; }
+                const double alpha = rho / pw;
+                for (long i = 0; i < N; ++i) { sol[i] += alpha * p[i]; r[i] += -alpha * q[i]; }
+                rnorm = pninf(L, r.data());
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                rho_1 = rho;
+            }
+        } else {
+            std::vector<double> p(N, 0.0), rh(r), v(N, 0.0), t(N);
+            double rho_1 = 0, alpha = 0, omega = 0;
+            for (int iter = 1; iter <= o.bottom_max_iter; ++iter) {
+                const double rho = dot(m, rh.data(), r.data());
+                if (rho == 0) { ret = 1; break; }
+                if (iter == 1) p = r;
+                else {
+                    const double beta = (rho / rho_1) * (alpha / omega);
+                    for (long i = 0; i < N; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+                }
+                papply(m, p.data(), v.data());
+                const double rhTv = dot(m, rh.data(), v.data());
+                if (rhTv != 0) alpha = rho / rhTv;
+                else { ret = 2; break; }
+                for (long i = 0; i < N; ++i) { sol[i] += alpha * p[i]; r[i] += -alpha * v[i]; }
+                rnorm = pninf(L, r.data());
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                papply(m, r.data(), t.data());
+                const double tt = dot(m, t.data(), t.data()), tr = dot(m, t.data(), r.data());
+                if (tt != 0) omega = tr / tt;
+                else { ret = 3; break; }
+                for (long i = 0; i < N; ++i) { sol[i] += omega * r[i]; r[i] += -omega * t[i]; }
+                rnorm = pninf(L, r.data());
+                if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+                if (omega == 0) { ret = 4; break; }
+                rho_1 = rho;
+            }
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+        if ((ret == 0 || ret == 8) && rnorm < rnorm0) {
+            for (long i = 0; i < N; ++i) sol[i] += sorig[i];
+        } else {
+            for (long i = 0; i < N; ++i) sol[i] = sorig[i];
+        }
+        return ret;
+    }
+    void bottom_solve() {
+        const int m = (int)lv.size() - 1;
+        double* x = lv[m].cor.data();
+        const double* b = lv[m].res.data();
+        std::fill(lv[m].cor.begin(), lv[m].cor.end(), 0.0);
+        const int ret = bottom_krylov(m, x, b);
+        if (ret != 0 && ret != 9) {
+            std::fill(lv[m].cor.begin(), lv[m].cor.end(), 0.0);
+            ++bottom_fail;
+        }
+        const int n = (ret == 0) ? 0 : o.nuf;
+        for (int i = 0; i < n; ++i) smooth(m, x, b);
+    }
+    void vcycle(int top) {
+        const int bot = (int)lv.size() - 1;
+        for (int m = top; m < bot; ++m) {
+            std::fill(lv[m].cor.begin(), lv[m].cor.end(), 0.0);
+            for (int i = 0; i < o.nu1; ++i) smooth(m, lv[m].cor.data(), lv[m].res.data());
+            res_of_cor(m);
+            prestrict(*lv[m + 1].L, *lv[m].L, 3, lv[m + 1].res.data(), lv[m].rescor.data());
+        }
+        bottom_solve();
+        for (int m = bot - 1; m >= top; --m) {
+            pinterp_add(*lv[m].L, *lv[m + 1].L, 3, lv[m].cor.data(), lv[m + 1].cor.data());
+            for (int i = 0; i < o.nu2; ++i) smooth(m, lv[m].cor.data(), lv[m].res.data());
+        }
+    }
+    void fcycle() {
+        const int bot = (int)lv.size() - 1;
+        for (int m = 1; m <= bot; ++m) prestrict(*lv[m].L, *lv[m - 1].L, 3, lv[m].res.data(), lv[m - 1].res.data());
+        bottom_solve();
+        for (int m = bot - 1; m >= 0; --m) {
+            std::fill(lv[m].cor.begin(), lv[m].cor.end(), 0.0);
+            pinterp_add(*lv[m].L, *lv[m + 1].L, 3, lv[m].cor.data(), lv[m + 1].cor.data());
+            res_of_cor(m);
+            lv[m].res = lv[m].rescor;
+            std::swap(lv[m].cor, lv[m].corhold);
+            vcycle(m);
+            for (size_t i = 0; i < lv[m].cor.size(); ++i) lv[m].cor[i] += lv[m].corhold[i];
+        }
+    }
+};
+
+// b = -sum_d (d_d C) : E e_d
+void prhs(const PLev& L, int model, const double* C, int uniform, const double E[9], double* B) {
+    double g[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) g[a][b] = E[3 * a + b];
+    for_cell(L, [&](int i, int j, int k) {
+        const long c = L.at(i, j, k);
+        double gc[3] = {0, 0, 0};
+        if (!uniform) pgradC(L, model, C, i, j, k, g, gc);
+        for (int p = 0; p < 3; ++p) B[p * L.nn + c] = -gc[p];
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_rve_num_mg_levels(const orc_rve_level* L, int max_mg_levels) {
+    orc_rve_level cur = *L;
+    int n = 1;
+    while (pcoarsenable(cur) && (max_mg_levels <= 0 || n < max_mg_levels)) {
+        for (int d = 0; d < 3; ++d) cur.n[d] /= 2;
+        ++n;
+    }
+    return n;
+}
+int orc_rve_fapply(const orc_rve_level* L, int model, const double* C, int uniform, const double* u, double* f) {
+    pfapply(PLev(*L), model, C, uniform, u, f);
+    return 0;
+}
+int orc_rve_diagonal(const orc_rve_level* L, int model, const double* C, double* diag) {
+    pdiagonal(PLev(*L), model, C, diag);
+    return 0;
+}
+int orc_rve_fsmooth(const orc_rve_level* L, int model, const double* C, int uniform, const double* diag, double* x,
+                    const double* b, int nsweeps, double omega) {
+    pfsmooth(PLev(*L), model, C, uniform, diag, x, b, nsweeps, omega);
+    return 0;
+}
+int orc_rve_residual(const orc_rve_level* L, int model, const double* C, int uniform, const double* x,
+                     const double* b, double* r, int project, double* mean, double* norm_inf) {
+    const double n = presidual(PLev(*L), model, C, uniform, x, b, r, project, mean);
+    if (norm_inf) *norm_inf = n;
+    return 0;
+}
+int orc_rve_restrict(const orc_rve_level* Lc, const orc_rve_level* Lf, int ncomp, double* crse, const double* fine) {
+    for (int d = 0; d < 3; ++d)
+        if (Lf->n[d] != 2 * Lc->n[d]) return -1;
+    prestrict(PLev(*Lc), PLev(*Lf), ncomp, crse, fine);
+    return 0;
+}
+int orc_rve_interp_add(const orc_rve_level* Lf, const orc_rve_level* Lc, int ncomp, double* fine,
+                       const double* crse) {
+    for (int d = 0; d < 3; ++d)
+        if (Lf->n[d] != 2 * Lc->n[d]) return -1;
+    pinterp_add(PLev(*Lf), PLev(*Lc), ncomp, fine, crse);
+    return 0;
+}
+int orc_rve_rhs(const orc_rve_level* L, int model, const double* C, int uniform, const double* E, double* b) {
+    prhs(PLev(*L), model, C, uniform, E, b);
+    return 0;
+}
+// cell average of the stress C : (E + grad w), grad w by central differences
+int orc_rve_mean_stress(const orc_rve_level* L0, int model, const double* C, const double* E, const double* w,
+                        double* sig) {
+    const PLev L(*L0);
+    const int nc = ncoef_of(model);
+    double acc[9] = {0};
+    for (int k = 0; k < L.n[2]; ++k)
+        for (int j = 0; j < L.n[1]; ++j)
+            for (int i = 0; i < L.n[0]; ++i) {
+                const long c = L.at(i, j, k);
+                double a[21], g[3][3], s[3][3];
+                for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
+                pgrad(L, w, i, j, k, g, nullptr);
+                for (int p = 0; p < 3; ++p)
+                    for (int d = 0; d < 3; ++d) g[p][d] += E[3 * p + d];
+                stress_of(model, a, g, s);
+                for (int p = 0; p < 3; ++p)
+                    for (int d = 0; d < 3; ++d) acc[3 * p + d] += s[p][d];
+            }
+    for (int q = 0; q < 9; ++q) sig[q] = acc[q] / (double)L.nn;
+    return 0;
+}
+// Cell solve: w (initial guess in, solution out, mean removed) for the macroscopic gradient E.
+// Convergence as MLMG (orc_solve_amr) on the mean-free residual; stats->res0/resfinal are those
+// norms.  body_force (3) receives the mean of the last residual.
+int orc_rve_solve(const orc_rve_level* L0, int model, const double* C, const double* E, double* w,
+                  double tol_rel, double tol_abs, const orc_opts* opts, orc_stats* stats, double* body_force) {
+    PSolver S;
+    S.model = model;
+    S.nc = ncoef_of(model);
+    S.o = *opts;
+    S.uniform = opts->uniform;
+    const int nlev = orc_rve_num_mg_levels(L0, opts->max_mg_levels);
+    S.lv.resize(nlev);
+    orc_rve_level cur = *L0;
+    for (int m = 0; m < nlev; ++m) {
+        if (m > 0)
+            for (int d = 0; d < 3; ++d) { cur.n[d] /= 2; cur.dx[d] *= 2.0; }
+        S.lv[m].ol = cur;
+        S.lv[m].L = new PLev(cur);
+        const long nn = S.lv[m].L->nn;
+        S.lv[m].C.assign(S.nc * nn, 0.0);
+        S.lv[m].D.assign(3 * nn, 0.0);
+        S.lv[m].res.assign(3 * nn, 0.0);
+        S.lv[m].cor.assign(3 * nn, 0.0);
+        S.lv[m].rescor.assign(3 * nn, 0.0);
+        S.lv[m].corhold.assign(3 * nn, 0.0);
+    }
+    const PLev& L = *S.lv[0].L;
+    std::memcpy(S.lv[0].C.data(), C, sizeof(double) * S.nc * L.nn);
+    for (int m = 1; m < nlev; ++m) prestrict(*S.lv[m].L, *S.lv[m - 1].L, S.nc, S.lv[m].C.data(), S.lv[m - 1].C.data());
+    for (int m = 0; m < nlev; ++m) pdiagonal(*S.lv[m].L, model, S.lv[m].C.data(), S.lv[m].D.data());
+
+    std::vector<double> b(3 * L.nn);
+    prhs(L, model, S.lv[0].C.data(), S.uniform, E, b.data());
+    double bm[3];
+    pmean(L, b.data(), bm);
+    psubtract(L, b.data(), bm);
+    const double bnorm = pninf(L, b.data());
+    double mu[3] = {0, 0, 0};
+    double* res0v = S.lv[0].res.data();
+    const double res0 = presidual(L, model, S.lv[0].C.data(), S.uniform, w, b.data(), res0v, 1, mu);
+    const double max_norm = (bnorm >= res0) ? bnorm : res0;
+    const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
+    int iters = 0, conv = 0;
+    double rn = res0;
+    if (res0 <= target) conv = 1;
+    for (int it = 0; !conv && it < opts->max_iter; ++it) {
+        if (it < opts->max_fmg_iter) S.fcycle();
+        else S.vcycle(0);
+        for (long i = 0; i < 3 * L.nn; ++i) w[i] += S.lv[0].cor[i];
+        rn = presidual(L, model, S.lv[0].C.data(), S.uniform, w, b.data(), res0v, 1, mu);
+        if (stats && it < 256) stats->hist[it] = rn;
+        iters = it + 1;
+        if (!(rn == rn)) break;
+        if (rn <= target) conv = 1;
+    }
+    double wm[3];
+    pmean(L, w, wm);
+    psubtract(L, w, wm);
+    if (body_force)
+        for (int p = 0; p < 3; ++p) body_force[p] = mu[p];
+    if (stats) {
+        stats->iters = iters;
+        stats->converged = conv;
+        stats->nlevels = nlev;
+        stats->bottom_fail = S.bottom_fail;
+        stats->res0 = res0;
+        stats->resfinal = rn;
+        stats->target = target;
+    }
+    return conv ? 0 : 1;
+}
+
+}  // extern "C"

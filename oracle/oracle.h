@@ -97,6 +97,33 @@ int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const*
 /* number of multigrid levels the solver builds for this level */
 int orc_num_mg_levels(const orc_level* L, int max_mg_levels);
 
+/* ---- periodic cells (homogenisation): n[0] n[1] n[2] unique nodes, no ghosts ----
+ * w periodic, u = E x + w; A w + c = b with b = -sum_d (d_d C) : E e_d, mean(w) = 0 and c a
+ * uniform body force (the multiplier of the mean constraint; see oracle.cpp). */
+typedef struct {
+    int n[3];
+    int pad_;
+    double dx[3];
+} orc_rve_level;
+
+int orc_rve_num_mg_levels(const orc_rve_level* L, int max_mg_levels);
+int orc_rve_fapply(const orc_rve_level* L, int model, const double* C, int uniform, const double* u, double* f);
+int orc_rve_diagonal(const orc_rve_level* L, int model, const double* C, double* diag);
+int orc_rve_fsmooth(const orc_rve_level* L, int model, const double* C, int uniform, const double* diag, double* x,
+                    const double* b, int nsweeps, double omega);
+/* r = b - A x; project != 0 removes the per-component mean (returned in mean[3]) */
+int orc_rve_residual(const orc_rve_level* L, int model, const double* C, int uniform, const double* x,
+                     const double* b, double* r, int project, double* mean, double* norm_inf);
+int orc_rve_restrict(const orc_rve_level* Lc, const orc_rve_level* Lf, int ncomp, double* crse, const double* fine);
+int orc_rve_interp_add(const orc_rve_level* Lf, const orc_rve_level* Lc, int ncomp, double* fine,
+                       const double* crse);
+/* E: 3x3 row-major displacement gradient */
+int orc_rve_rhs(const orc_rve_level* L, int model, const double* C, int uniform, const double* E, double* b);
+int orc_rve_mean_stress(const orc_rve_level* L, int model, const double* C, const double* E, const double* w,
+                        double* sig);
+int orc_rve_solve(const orc_rve_level* L, int model, const double* C, const double* E, double* w,
+                  double tol_rel, double tol_abs, const orc_opts* opts, orc_stats* stats, double* body_force);
+
 #ifdef __cplusplus
 }
 #endif

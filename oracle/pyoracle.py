@@ -263,3 +263,120 @@ def node_coords(L):
     ax = [(np.arange(L.lo[d] - L.ng, L.hi[d] + L.ng + 1)) * L.dx[d] for d in range(3)]
     Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
     return X, Y, Z
+
+
+# ---------------------------------------------------------------- periodic cells
+class RveLevel(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("pad_", C.c_int), ("dx", C.c_double * 3)]
+
+    @property
+    def shape(self):
+        return (self.n[2], self.n[1], self.n[0])
+
+
+def _rve_lib():
+    lb = lib()
+    if not getattr(lb, "_rve_ready", False):
+        d = C.POINTER(C.c_double)
+        R = C.POINTER(RveLevel)
+        lb.orc_rve_num_mg_levels.argtypes = [R, C.c_int]
+        lb.orc_rve_fapply.argtypes = [R, C.c_int, d, C.c_int, d, d]
+        lb.orc_rve_diagonal.argtypes = [R, C.c_int, d, d]
+        lb.orc_rve_fsmooth.argtypes = [R, C.c_int, d, C.c_int, d, d, d, C.c_int, C.c_double]
+        lb.orc_rve_residual.argtypes = [R, C.c_int, d, C.c_int, d, d, d, C.c_int, d, d]
+        lb.orc_rve_restrict.argtypes = [R, R, C.c_int, d, d]
+        lb.orc_rve_interp_add.argtypes = [R, R, C.c_int, d, d]
+        lb.orc_rve_rhs.argtypes = [R, C.c_int, d, C.c_int, d, d]
+        lb.orc_rve_mean_stress.argtypes = [R, C.c_int, d, d, d, d]
+        lb.orc_rve_solve.argtypes = [R, C.c_int, d, d, d, C.c_double, C.c_double, C.POINTER(Opts),
+                                     C.POINTER(Stats), d]
+        lb._rve_ready = True
+    return lb
+
+
+def rve_level(n, length=1.0):
+    """Periodic cell of n (int or 3 ints) cells per side on a cube of edge `length`."""
+    n = (n,) * 3 if np.isscalar(n) else tuple(n)
+    L = RveLevel()
+    for d in range(3):
+        L.n[d] = n[d]
+        L.dx[d] = length / n[d]
+    return L
+
+
+def rve_coarsen(L):
+    Lc = RveLevel()
+    for d in range(3):
+        Lc.n[d] = L.n[d] // 2
+        Lc.dx[d] = 2.0 * L.dx[d]
+    return Lc
+
+
+def rve_num_mg_levels(L, max_mg_levels=0):
+    return _rve_lib().orc_rve_num_mg_levels(C.byref(L), max_mg_levels)
+
+
+def rve_fapply(L, model, Cf, u, uniform=False):
+    f = np.zeros((3,) + L.shape)
+    _rve_lib().orc_rve_fapply(C.byref(L), model, _d(Cf), int(uniform), _d(np.ascontiguousarray(u)), _d(f))
+    return f
+
+
+def rve_diagonal(L, model, Cf):
+    D = np.zeros((3,) + L.shape)
+    _rve_lib().orc_rve_diagonal(C.byref(L), model, _d(Cf), _d(D))
+    return D
+
+
+def rve_fsmooth(L, model, Cf, diag, x, b, nsweeps=2, omega=2.0 / 3.0, uniform=False):
+    x = x.copy()
+    _rve_lib().orc_rve_fsmooth(C.byref(L), model, _d(Cf), int(uniform), _d(diag), _d(x), _d(b), nsweeps, omega)
+    return x
+
+
+def rve_residual(L, model, Cf, x, b, project=True, uniform=False):
+    r = np.zeros((3,) + L.shape)
+    mean = np.zeros(3)
+    nrm = C.c_double()
+    _rve_lib().orc_rve_residual(C.byref(L), model, _d(Cf), int(uniform), _d(x), _d(b), _d(r), int(project),
+                                _d(mean), C.cast(C.byref(nrm), C.POINTER(C.c_double)))
+    return r, mean, nrm.value
+
+
+def rve_restrict(Lc, Lf, fine):
+    ncomp = fine.shape[0]
+    c = np.zeros((ncomp,) + Lc.shape)
+    assert _rve_lib().orc_rve_restrict(C.byref(Lc), C.byref(Lf), ncomp, _d(c), _d(np.ascontiguousarray(fine))) == 0
+    return c
+
+
+def rve_interp_add(Lf, Lc, fine, crse):
+    fine = fine.copy()
+    assert _rve_lib().orc_rve_interp_add(C.byref(Lf), C.byref(Lc), fine.shape[0], _d(fine),
+                                         _d(np.ascontiguousarray(crse))) == 0
+    return fine
+
+
+def rve_rhs(L, model, Cf, E, uniform=False):
+    b = np.zeros((3,) + L.shape)
+    _rve_lib().orc_rve_rhs(C.byref(L), model, _d(Cf), int(uniform),
+                           _d(np.ascontiguousarray(E, dtype=np.float64).reshape(9)), _d(b))
+    return b
+
+
+def rve_mean_stress(L, model, Cf, E, w):
+    s = np.zeros(9)
+    _rve_lib().orc_rve_mean_stress(C.byref(L), model, _d(Cf), _d(np.ascontiguousarray(E, dtype=np.float64).reshape(9)),
+                                   _d(np.ascontiguousarray(w)), _d(s))
+    return s.reshape(3, 3)
+
+
+def rve_solve(L, model, Cf, E, w0=None, tol_rel=1e-8, tol_abs=0.0, **kw):
+    """Periodic cell solve; returns (w with zero mean, stats, rc, body force)."""
+    w = np.zeros((3,) + L.shape) if w0 is None else w0.copy()
+    o = default_opts(**kw)
+    st = Stats()
+    bf = np.zeros(3)
+    rc = _rve_lib().orc_rve_solve(C.byref(L), model, _d(Cf), _d(np.ascontiguousarray(E, dtype=np.float64).reshape(9)),
+                                  _d(w), tol_rel, tol_abs, C.byref(o), C.byref(st), _d(bf))
+    return w, st, rc, bf

@@ -45,8 +45,9 @@ def test_struct_layouts_match_header():
 #include <stddef.h>
 #include "aefast.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu\n", sizeof(ae_level_desc), sizeof(ae_fab), sizeof(ae_solver_opts),
-         sizeof(ae_solve_stats), offsetof(ae_solver_opts, omega));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ae_level_desc), sizeof(ae_fab), sizeof(ae_solver_opts),
+         sizeof(ae_solve_stats), offsetof(ae_solver_opts, omega), sizeof(ae_cell_desc), sizeof(ae_cell_stats),
+         offsetof(ae_cell_stats, mean_stress));
   return 0;
 }
 """
@@ -58,7 +59,8 @@ int main(void) {
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
     sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert sizes == [C.sizeof(_lib.LevelDesc), C.sizeof(_lib.Fab), C.sizeof(_lib.SolverOpts),
-                     C.sizeof(_lib.SolveStats), _lib.SolverOpts.omega.offset]
+                     C.sizeof(_lib.SolveStats), _lib.SolverOpts.omega.offset, C.sizeof(_lib.CellDesc),
+                     C.sizeof(_lib.CellStats), _lib.CellStats.mean_stress.offset]
 
 
 def test_host_only_entry_points(lib):
