@@ -289,16 +289,18 @@ void CellEngine::rebuild() {
     if (ncell) AEH_CHECK(cudaMemcpyAsync(dcells, hcells.data(), sizeof(CellDev) * ncell, cudaMemcpyHostToDevice, st));
     if (nsolves)
         AEH_CHECK(cudaMemcpyAsync(dsolves, hsolves.data(), sizeof(SolveDev) * nsolves, cudaMemcpyHostToDevice, st));
-    // work tables
+    // work tables: runs ordered cell, run, load case, so that the load cases of a cell read the
+    // same stiffness run back to back (one HBM read, the rest from L2)
     for (int ci = 0; ci < 2; ++ci) {
         const int chunk = ci == 0 ? 128 : 256;
         for (int m = 0; m < kMaxCellLevels; ++m) {
             Table& T = tall[ci][m];
             T.h.clear();
-            for (int s = 0; s < nsolves; ++s) {
-                const CellRes* r = live[hsolves[s].cell];
+            for (int c = 0; c < ncell; ++c) {
+                const CellRes* r = live[c];
                 if (m >= r->nlev) continue;
-                for (int t0 = 0; t0 < r->lv[m].nn; t0 += chunk) T.h.push_back(Work{s, t0});
+                for (int t0 = 0; t0 < r->lv[m].nn; t0 += chunk)
+                    for (int k = 0; k < r->nrhs; ++k) T.h.push_back(Work{solve_base[c] + k, t0});
             }
             T.upload(st);
         }
