@@ -87,6 +87,13 @@ struct MGLevel {
     double *res = nullptr, *cor = nullptr, *rescor = nullptr, *corhold = nullptr, *tmp = nullptr;
     float *C32 = nullptr, *D32 = nullptr, *invD32 = nullptr;
     float *res32 = nullptr, *cor32 = nullptr, *rescor32 = nullptr, *corhold32 = nullptr, *tmp32 = nullptr;
+    // Voronoi stiffness (finest MG level of an AMR level, ae_op_set_model_grains): grain id per
+    // node laid out like C, per-grain tables; the sweeps read these instead of C / C32
+    unsigned short* gid = nullptr;
+    double* gtab64 = nullptr;
+    float* gtab32 = nullptr;
+    int ngrains = 0, gcap = 0;
+    bool grains = false;
 };
 
 struct AmrLevel {
@@ -150,6 +157,21 @@ struct ae_op_s {
         P.model = model;
         P.uniform = uniform;
         return P;
+    }
+    // the grain tables of the level whose stiffness array is C, if it has them
+    template <class R>
+    Grains<R> grains_for(const R* C) const {
+        Grains<R> G;
+        for (const AmrLevel& A : amr) {
+            const MGLevel& L = A.mg[0];
+            if (!L.grains) continue;
+            if constexpr (sizeof(R) == 8) {
+                if (C == L.C) { G.gid = L.gid; G.tab = L.gtab64; }
+            } else {
+                if (C == L.C32) { G.gid = L.gid; G.tab = L.gtab32; }
+            }
+        }
+        return G;
     }
 };
 
@@ -347,7 +369,8 @@ void sweep_jacobi(ae_op* op, const Geo& g, const R* C, const R* invD, const R* D
     else
         launch_jacobi<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(invD))),
                          cview(level_view(g, const_cast<R*>(D))), cview(level_view(g, const_cast<R*>(xi))),
-                         cview(level_view(g, const_cast<R*>(b))), level_view(g, xo), omega, st);
+                         cview(level_view(g, const_cast<R*>(b))), level_view(g, xo), omega, st,
+                         op->grains_for<R>(C));
 }
 // r = b - A x on internal buffers (no norm); r may alias b
 template <class R>
@@ -359,7 +382,8 @@ void sweep_residual(ae_op* op, const Geo& g, const R* C, const R* x, const R* b,
                         cview(level_view(g, const_cast<R*>(b))), level_view(g, r), R(0), st);
     else
         launch_residual<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
-                           cview(level_view(g, const_cast<R*>(b))), level_view(g, r), nullptr, nullptr, st);
+                           cview(level_view(g, const_cast<R*>(b))), level_view(g, r), nullptr, nullptr, st,
+                           op->grains_for<R>(C));
 }
 template <class R>
 void sweep_fapply(ae_op* op, const Geo& g, const R* C, const R* x, R* f, cudaStream_t st) {
@@ -370,7 +394,7 @@ void sweep_fapply(ae_op* op, const Geo& g, const R* C, const R* x, R* f, cudaStr
                         cview(level_view(g, const_cast<R*>(x))), level_view(g, f), R(0), st);
     else
         launch_fapply<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
-                         level_view(g, f), st);
+                         level_view(g, f), st, op->grains_for<R>(C));
 }
 
 // ------------------------------------------------------------------ the multigrid cycle
@@ -586,7 +610,7 @@ void ml_residual64(ae_op* op, const ae_solver_opts& o) {
         View<float> r32 = o.precision ? level_view(L.g, L.res32) : View<float>{};
         launch_residual<double>(op->params(L.g), cview(level_view(L.g, L.C)), it.CV(0, it.sol[0]),
                                 it.CV(0, it.rhs[0]), level_view(L.g, L.res), op->dnorm, o.precision ? &r32 : nullptr,
-                                st);
+                                st, op->grains_for<double>(L.C));
         return;
     }
     it.ml_residual();
@@ -864,6 +888,48 @@ int ae_op_set_model(ae_op* op, int amrlev, const ae_fab* coeffs) {
         View<const double> src = device_view_in(op, *coeffs, 0);
         launch_copy<double, double>(need, op->ncoef, level_view(L.g, L.C), src, op->st);
         AE_CHECK(cudaStreamSynchronize(op->st));
+        L.grains = false;
+        op->amr[amrlev].model_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_model_grains(ae_op* op, int amrlev, const ae_fab* grain_id, int ngrains, const double* table) {
+    return guarded([&] {
+        require(op != nullptr && table != nullptr, "null argument");
+        require(ngrains >= 1 && ngrains <= 65535, "SetModelGrains: 1 to 65535 grains");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 need = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        check_fab(grain_id, need, 1, "SetModelGrains");
+        View<const int> ids;
+        if (is_device_ptr(grain_id->data)) {
+            ids = cview(fab_view<int>(*grain_id));
+        } else {
+            const size_t bytes = sizeof(int) * (size_t)box_npts(fab_box(*grain_id));
+            ensure_stage(op->stage, op->stage_bytes, bytes);
+            AE_CHECK(cudaMemcpyAsync(op->stage, grain_id->data, bytes, cudaMemcpyHostToDevice, op->st));
+            ae_fab d = *grain_id;
+            d.data = op->stage;
+            ids = cview(fab_view<int>(d));
+        }
+        const int nc = op->ncoef;
+        if (!L.gid) L.gid = op->alloc<unsigned short>(L.nn);
+        if (L.gcap < ngrains) {
+            L.gtab64 = op->alloc<double>((long long)ngrains * nc);
+            L.gtab32 = op->alloc<float>((long long)ngrains * nc);
+            L.gcap = ngrains;
+        }
+        AE_CHECK(cudaMemcpyAsync(L.gtab64, table, sizeof(double) * ngrains * nc, cudaMemcpyDefault, op->st));
+        AE_CHECK(cudaMemsetAsync(op->dflag, 0, sizeof(int), op->st));
+        launch_grains_box(need, ids, level_view(L.g, L.gid), level_view(L.g, L.C), L.gtab64, ngrains, nc, L.gtab32,
+                          op->dflag, op->st);
+        int bad = 0;
+        AE_CHECK(cudaMemcpyAsync(&bad, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, op->st));
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        require(bad == 0, "SetModelGrains: a grain id is outside [0, ngrains)");
+        L.ngrains = ngrains;
+        L.grains = true;
         op->amr[amrlev].model_set = true;
         op->prepared = false;
     });
@@ -881,6 +947,7 @@ int ae_op_set_model_uniform(ae_op* op, const double* coeffs, int ncoef) {
                 for (long long n = 0; n < L.nn; ++n) host[(size_t)q * L.nn + n] = coeffs[q];
             AE_CHECK(cudaMemcpyAsync(L.C, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, op->st));
             AE_CHECK(cudaStreamSynchronize(op->st));
+            L.grains = false;
             op->amr[a].model_set = true;
         }
         op->prepared = false;
@@ -964,12 +1031,12 @@ int ae_fapply(ae_op* op, int amrlev, int mglev, const ae_fab* out, const ae_fab*
             if (op->tiled32) tiled(0.0f);
             else
                 launch_fapply<float>(P, cview(level_view(L.g, L.C32)), cview(fab_view<float>(*in)),
-                                     fab_view<float>(*out), op->st);
+                                     fab_view<float>(*out), op->st, op->grains_for<float>(L.C32));
         } else {
             if (op->tiled64) tiled(0.0);
             else
                 launch_fapply<double>(P, cview(level_view(L.g, L.C)), cview(fab_view<double>(*in)),
-                                      fab_view<double>(*out), op->st);
+                                      fab_view<double>(*out), op->st, op->grains_for<double>(L.C));
         }
     });
 }
@@ -1038,7 +1105,8 @@ int ae_residual(ae_op* op, int amrlev, int mglev, const ae_fab* r, const ae_fab*
                 "residual: fabs must be device memory");
         AE_CHECK(cudaMemsetAsync(op->dnorm, 0, sizeof(unsigned long long), op->st));
         launch_residual<double>(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*x)),
-                                cview(fab_view<double>(*b)), fab_view<double>(*r), op->dnorm, nullptr, op->st);
+                                cview(fab_view<double>(*b)), fab_view<double>(*r), op->dnorm, nullptr, op->st,
+                                op->grains_for<double>(L.C));
         const double n = read_norm(op, 0);
         if (norm_inf) *norm_inf = n;
     });

@@ -90,6 +90,44 @@ __device__ __forceinline__ void cell_apply(const SCoef<R>& K, bool uniform, cons
     }
 }
 
+// f = A u at node t of a Voronoi cell stored as a grain id per node and a per-grain coefficient
+// table (tab[g * ncoef + q]).  The arithmetic is that of cell_apply on the equivalent per-node
+// field; a direction whose two neighbours lie in the same grain has an exactly zero stiffness
+// difference, so its column of the grad C term is zero and its loads are skipped.
+template <int M, class R>
+__device__ __forceinline__ void cell_apply_grains(const SCoef<R>& K, bool uniform,
+                                                  const unsigned short* __restrict__ gid,
+                                                  const R* __restrict__ tab, const R* __restrict__ U, int us, int t,
+                                                  const POff& o, R f[3]) {
+    constexpr int NC = NCoef<M>::value;
+    R gu[3][3], b[3][3][3];
+    cell_derivs<R>(K, U, us, t, o, gu, b);
+    {
+        const R* a0 = tab + (int)__ldg(gid + t) * NC;
+        R a[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) a[q] = __ldg(a0 + q);
+        div_of<M, R>(a, b, f);
+    }
+    if (!uniform) {
+        const int gp[3] = {__ldg(gid + t + o.xp), __ldg(gid + t + o.yp), __ldg(gid + t + o.zp)};
+        const int gm[3] = {__ldg(gid + t + o.xm), __ldg(gid + t + o.ym), __ldg(gid + t + o.zm)};
+        R col[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (gp[d] == gm[d]) {
+                col[d][0] = col[d][1] = col[d][2] = R(0);
+            } else {
+                const R* cp = tab + gp[d] * NC;
+                const R* cm = tab + gm[d] * NC;
+                gradC_col_f<M, R>([&](int q) { return __ldg(cp + q) - __ldg(cm + q); }, gu, d, col[d]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) f[r] += (col[0][r] * K.h[0] + col[1][r] * K.h[1]) + col[2][r] * K.h[2];
+    }
+}
+
 // interior diagonal (src/Operator/Elastic.cpp:320-341): C_{pjpj} (-2 / dx_j^2)
 template <int M, class R>
 __device__ __forceinline__ void cell_diag(const SCoef<R>& K, const R* __restrict__ C, int cs, int t, R d[3]) {

@@ -76,9 +76,17 @@ size_t cell_layout(CellRes& c, char* base) {
         L.I32 = (float*)take(sizeof(float) * 3 * nn);
         L.K64 = scoef_dx<double>(dx);
         L.K32 = scoef_dx<float>(dx);
+        L.gid = nullptr;
+        L.ngrains = 0;
+        L.tab64 = nullptr;
+        L.tab32 = nullptr;
+        L.dtab64 = nullptr;
+        L.itab64 = nullptr;
+        L.itab32 = nullptr;
         for (int d = 0; d < 3; ++d) { n[d] /= 2; dx[d] *= 2.0; }
     }
     const size_t nn0 = (size_t)c.lv[0].nn, nnb = (size_t)c.lv[c.nlev - 1].nn;
+    c.gid_mem = (unsigned short*)take(sizeof(unsigned short) * nn0);
     const size_t nch = (nn0 + kRedChunk - 1) / kRedChunk;
     c.sol.assign(c.nrhs, SolveDev{});
     for (int r = 0; r < c.nrhs; ++r) {
@@ -242,7 +250,60 @@ CellRes* CellEngine::new_cell(const int n[3], const double len[3], int nrhs) {
 void CellEngine::free_cell(CellRes* c) {
     if (!c) return;
     if (c->mem) cudaFreeAsync(c->mem, st);
+    if (c->gtab) cudaFreeAsync(c->gtab, st);
     delete c;
+}
+
+void CellEngine::set_grains(CellRes* c, int ng, const double* seeds, const double* table) {
+    require(ng >= 1 && ng <= 65535, "grains: 1 to 65535 grains");
+    require(seeds && table, "grains: seeds and table required");
+    CellLevelDev& L = c->lv[0];
+    if (c->gtab) AEH_CHECK(cudaFreeAsync(c->gtab, st));
+    c->gtab = nullptr;
+    // tables: stiffness FP64 and FP32, diagonal FP64, 1/diagonal FP64 and FP32
+    const size_t n64 = (size_t)ng * nc, n32 = n64;
+    const size_t bytes = align256(8 * n64) + align256(4 * n32) + 3 * align256(8 * 3 * (size_t)ng);
+    void* mem = nullptr;
+    AEH_CHECK(cudaMallocAsync(&mem, bytes, st));
+    c->gtab = mem;
+    char* p = (char*)mem;
+    L.tab64 = (double*)p;
+    p += align256(8 * n64);
+    L.tab32 = (float*)p;
+    p += align256(4 * n32);
+    L.dtab64 = (double*)p;
+    p += align256(8 * 3 * (size_t)ng);
+    L.itab64 = (double*)p;
+    p += align256(8 * 3 * (size_t)ng);
+    L.itab32 = (float*)p;
+    L.ngrains = ng;
+    L.gid = c->gid_mem;
+    void* sbuf = nullptr;
+    AEH_CHECK(cudaMallocAsync(&sbuf, sizeof(double) * 3 * ng, st));
+    AEH_CHECK(cudaMemcpyAsync(sbuf, seeds, sizeof(double) * 3 * ng, cudaMemcpyDefault, st));
+    AEH_CHECK(cudaMemcpyAsync(L.tab64, table, sizeof(double) * n64, cudaMemcpyDefault, st));
+    cells_launch_grains(model, L, c->len, (const double*)sbuf, ng, L.tab64, st);
+    AEH_CHECK(cudaFreeAsync(sbuf, st));
+    AEH_CHECK(cudaStreamSynchronize(st));
+    c->model_set = true;
+    c->prepared = false;
+}
+
+void CellEngine::set_field(CellRes* c, const void* C) {
+    CellLevelDev& L = c->lv[0];
+    L.gid = nullptr;
+    L.ngrains = 0;
+    L.tab64 = nullptr;
+    L.tab32 = nullptr;
+    L.dtab64 = nullptr;
+    L.itab64 = nullptr;
+    L.itab32 = nullptr;
+    if (c->gtab) AEH_CHECK(cudaFreeAsync(c->gtab, st));
+    c->gtab = nullptr;
+    AEH_CHECK(cudaMemcpyAsync(L.C64, C, sizeof(double) * nc * (size_t)L.nn, cudaMemcpyDefault, st));
+    AEH_CHECK(cudaStreamSynchronize(st));
+    c->model_set = true;
+    c->prepared = false;
 }
 
 void CellEngine::rebuild() {
@@ -252,6 +313,7 @@ void CellEngine::rebuild() {
     hsolves.clear();
     solve_base.assign(ncell, 0);
     maxL = 0;
+    reps0 = 0;
     for (int c = 0; c < ncell; ++c) {
         CellRes* r = live[c];
         CellDev& d = hcells[c];
@@ -266,6 +328,7 @@ void CellEngine::rebuild() {
             hsolves.push_back(s);
         }
         maxL = std::max(maxL, r->nlev);
+        reps0 |= r->lv[0].gid ? 2 : 1;
     }
     nsolves = (int)hsolves.size();
     if ((size_t)ncell > cap_cells || !dcells) {
@@ -388,7 +451,7 @@ void CellEngine::begin(const std::vector<int>& cell_slots, const ae_solver_opts&
     cells_launch_rhs(model, A, tsub.d, tsub.n, st);
     cells_launch_mean(A, dslots, ns, 0, 1, st);
     cells_launch_project(prec, 1, A, tsub.d, tsub.n, st);
-    cells_launch_resid_top(model, A, tsub.d, tsub.n, st);
+    cells_launch_resid_top(model, A, tsub.d, tsub.n, reps0, st);
     cells_launch_mean(A, dslots, ns, 0, 0, st);
     cells_launch_project(prec, 0, A, tsub.d, tsub.n, st);
     cells_launch_status(A, dslots, ns, 1, tol_rel, tol_abs, o.max_iter, dcount, nullptr, st);
@@ -406,7 +469,7 @@ void CellEngine::smooth_phase(int prec, int m, int calls, bool zero, const ae_so
     }
     int from2 = 0;
     for (int s = 0; s < total; ++s) {
-        cells_launch_smooth(model, prec, zero && s == 0, A, T.d, T.n, sh, m, from2, st);
+        cells_launch_smooth(model, prec, zero && s == 0, A, T.d, T.n, sh, m, from2, reps(m), st);
         from2 ^= 1;
     }
     if (from2) cells_launch_copy2(prec, A, T.d, T.n, sh, m, st);
@@ -416,7 +479,7 @@ void CellEngine::vcycle(int prec, const ae_solver_opts& o) {
     const CellArgs A = args(o);
     for (int m = 0; m + 1 < maxL; ++m) {
         smooth_phase(prec, m, o.nu1, true, o, A);
-        cells_launch_rescor(model, prec, A, table(m).d, table(m).n, shape(m), m, 0, st);
+        cells_launch_rescor(model, prec, A, table(m).d, table(m).n, shape(m), m, 0, reps(m), st);
         cells_launch_restrict(prec, A, table(m + 1).d, table(m + 1).n, shape(m + 1), m, st);
     }
     const KrylovParams kp{o.bottom, o.bottom_max_iter, o.bottom_reltol, o.nuf};
@@ -434,9 +497,9 @@ void CellEngine::iteration_body(int prec, const ae_solver_opts& o, double tol_re
     for (int c = 0; c < inner; ++c) {
         vcycle(prec, o);
         cells_launch_update(prec, A, tred.d, tred.n, st);
-        if (c + 1 < inner) cells_launch_rescor(model, prec, A, table(0).d, table(0).n, shape(0), 0, 1, st);
+        if (c + 1 < inner) cells_launch_rescor(model, prec, A, table(0).d, table(0).n, shape(0), 0, 1, reps0, st);
     }
-    cells_launch_resid_top(model, A, tred.d, tred.n, st);
+    cells_launch_resid_top(model, A, tred.d, tred.n, reps0, st);
     cells_launch_mean(A, nullptr, nsolves, 0, 0, st);
     cells_launch_project(prec, 0, A, tred.d, tred.n, st);
     cells_launch_status(A, nullptr, nsolves, 0, tol_rel, tol_abs, o.max_iter, dcount, dactive, st);
@@ -536,9 +599,10 @@ void CellEngine::tune(int prec, const ae_solver_opts& o) {
                 sh.chunk = ci == 0 ? 128 : 256;
                 sh.grid = mu == 0 ? T.n : std::min(T.n, nsm * mu);
                 if (mu != 0 && sh.grid == T.n) continue;
-                cells_launch_smooth(model, prec, false, A, T.d, T.n, sh, m, 0, st);  // warm
+                cells_launch_smooth(model, prec, false, A, T.d, T.n, sh, m, 0, reps(m), st);  // warm
                 AEH_CHECK(cudaEventRecord(e0, st));
-                for (int r = 0; r < 3; ++r) cells_launch_smooth(model, prec, false, A, T.d, T.n, sh, m, 0, st);
+                for (int r = 0; r < 3; ++r)
+                    cells_launch_smooth(model, prec, false, A, T.d, T.n, sh, m, 0, reps(m), st);
                 AEH_CHECK(cudaEventRecord(e1, st));
                 AEH_CHECK(cudaEventSynchronize(e1));
                 float ms = 0.f;
@@ -659,11 +723,7 @@ int ae_batch_set_model(ae_batch b, int cell, const ae_fab* C) {
     return hx::guarded([&] {
         CellRes* c = cell_of(b, cell);
         fab_cell_check(C, c, c->nc, "ae_batch_set_model");
-        const size_t bytes = sizeof(double) * c->nc * (size_t)c->lv[0].nn;
-        AEH_CHECK(cudaMemcpyAsync(c->lv[0].C64, C->data, bytes, cudaMemcpyDefault, b->eng.st));
-        AEH_CHECK(cudaStreamSynchronize(b->eng.st));
-        c->model_set = true;
-        c->prepared = false;
+        b->eng.set_field(c, C->data);
         b->prepared = false;
     });
 }
@@ -671,18 +731,7 @@ int ae_batch_set_model(ae_batch b, int cell, const ae_fab* C) {
 int ae_batch_set_model_grains(ae_batch b, int cell, int ngrains, const double* seeds, const double* table) {
     return hx::guarded([&] {
         CellRes* c = cell_of(b, cell);
-        require(ngrains >= 1 && seeds && table, "ae_batch_set_model_grains: need ngrains >= 1, seeds and table");
-        const size_t ns = sizeof(double) * 3 * ngrains, nt = sizeof(double) * c->nc * ngrains;
-        void* buf = nullptr;
-        AEH_CHECK(cudaMallocAsync(&buf, ns + nt, b->eng.st));
-        AEH_CHECK(cudaMemcpyAsync(buf, seeds, ns, cudaMemcpyDefault, b->eng.st));
-        AEH_CHECK(cudaMemcpyAsync((char*)buf + ns, table, nt, cudaMemcpyDefault, b->eng.st));
-        cells_launch_grains(b->eng.model, c->lv[0], c->len, (const double*)buf, ngrains,
-                            (const double*)((char*)buf + ns), b->eng.st);
-        AEH_CHECK(cudaFreeAsync(buf, b->eng.st));
-        AEH_CHECK(cudaStreamSynchronize(b->eng.st));
-        c->model_set = true;
-        c->prepared = false;
+        b->eng.set_grains(c, ngrains, seeds, table);
         b->prepared = false;
     });
 }
@@ -702,6 +751,7 @@ int ae_batch_prepare(ae_batch b) {
     return hx::guarded([&] {
         require(b != nullptr, "null batch");
         for (CellRes* c : b->cells) require(c->model_set, "the model of every cell must be set", AE_ERR_STATE);
+        b->eng.rebuild();  // descriptors carry each cell's finest-level representation
         for (CellRes* c : b->cells)
             if (!c->prepared) b->eng.prepare_cell(c);
         b->prepared = true;

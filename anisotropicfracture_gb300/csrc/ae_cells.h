@@ -29,6 +29,16 @@ struct CellLevelDev {
     float* I32;
     SCoef<double> K64;
     SCoef<float> K32;
+    // Voronoi cells, finest level only: grain id per node and per-grain tables of the stiffness
+    // (ncoef), diagonal and 1/diagonal (3).  gid == nullptr: per-node arrays only.  The kernels of
+    // the finest level read these instead of the per-node arrays (same values, far fewer bytes).
+    unsigned short* gid;
+    int ngrains;
+    double* tab64;
+    float* tab32;
+    double* dtab64;
+    double* itab64;
+    float* itab32;
 };
 struct CellDev {
     int nlev;
@@ -92,13 +102,16 @@ struct Shape {
 };
 
 // ---- launchers (ae_cells_kernels.cu); model 0 ISO, 1 MM, 2 DIAG
+// reps (stencil launchers): bit 0 runs the per-node variant, bit 1 the grain-table variant; on
+// the finest level each entry is served by the variant that matches its cell, coarser levels
+// always take the per-node variant (reps = 1).
 void cells_launch_smooth(int model, int prec, bool zero, const CellArgs& A, const Work* tab, int ntab, Shape sh,
-                         int m, int from2, cudaStream_t st);
+                         int m, int from2, int reps, cudaStream_t st);
 void cells_launch_copy2(int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m, cudaStream_t st);
 void cells_launch_fill0(int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m, cudaStream_t st);
 // rescor_m = res_m - A cor_m (inplace: res_m -= A cor_m)
 void cells_launch_rescor(int model, int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m,
-                         int inplace, cudaStream_t st);
+                         int inplace, int reps, cudaStream_t st);
 // res_{m+1} = R rescor_m, tab over level m+1 nodes
 void cells_launch_restrict(int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m, cudaStream_t st);
 // cor_m += I cor_{m+1}, tab over level m nodes
@@ -106,7 +119,7 @@ void cells_launch_interp(int prec, const CellArgs& A, const Work* tab, int ntab,
 void cells_launch_bottom(int model, int prec, const CellArgs& A, int nsolves, const KrylovParams& kp,
                          cudaStream_t st);
 // FP64 top level (tab: level-0 runs of kRedChunk nodes, one block each)
-void cells_launch_resid_top(int model, const CellArgs& A, const Work* tab, int ntab, cudaStream_t st);
+void cells_launch_resid_top(int model, const CellArgs& A, const Work* tab, int ntab, int reps, cudaStream_t st);
 void cells_launch_rhs(int model, const CellArgs& A, const Work* tab, int ntab, cudaStream_t st);
 // per-solve mean of the partials: which 0 residual/rhs -> mean, 1 w -> wmean, 2 stress -> sig
 // (slots: the solve slots to visit, nullptr = 0 .. nsolves-1)
@@ -127,7 +140,8 @@ void cells_launch_zero_x(const CellArgs& A, const Work* tab, int ntab, cudaStrea
 // cell set-up (tab over cell ids): C_{m} = R C_{m-1}; D, 1/D, FP32 copies; NaN flag
 void cells_launch_coarsen_C(int model, const CellArgs& A, const Work* tab, int ntab, int m, cudaStream_t st);
 // level-0 stiffness of a Voronoi cell from seeds (ng x 3, in the cell's length units) and a
-// per-grain coefficient table (ng x ncoef); device pointers
+// per-grain coefficient table (ng x ncoef); device pointers.  When L.gid is set, also the grain
+// ids and L's grain tables (L.tab64 must hold the table, L.ngrains = ng).
 void cells_launch_grains(int model, const CellLevelDev& L, const double len[3], const double* seeds, int ng,
                          const double* table, cudaStream_t st);
 void cells_launch_diag(int model, const CellArgs& A, const Work* tab, int ntab, int m, int* nan_flag, cudaStream_t st);

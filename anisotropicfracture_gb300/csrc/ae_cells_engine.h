@@ -22,6 +22,8 @@ struct CellRes {
     int nc = 0;
     char* mem = nullptr;
     size_t bytes = 0;
+    unsigned short* gid_mem = nullptr;  // grain ids of the finest level (inside mem)
+    void* gtab = nullptr;               // grain tables of a Voronoi cell (own allocation)
     CellLevelDev lv[kMaxCellLevels];
     std::vector<SolveDev> sol;
     std::vector<std::array<double, 9>> E;
@@ -57,6 +59,8 @@ struct CellEngine {
     SolveDev* dsolves = nullptr;
     size_t cap_solves = 0;
     int nsolves = 0, maxL = 0;
+    int reps0 = 1;  // finest-level representations present (bit 0 per-node, bit 1 grain tables)
+    int reps(int m) const { return m == 0 ? reps0 : 1; }
     std::vector<int> solve_base;  // first solve slot of each cell slot
     // tables: per chunk option (128, 256) and level, solves; level-0 reduction runs; cells
     Table tall[2][kMaxCellLevels];
@@ -98,6 +102,11 @@ struct CellEngine {
     void upload_loads();  // E of every solve
     // coarsen the stiffness, diagonals, FP32 copies of a cell; NaN/zero-diagonal check
     void prepare_cell(CellRes* c);
+    // finest-level stiffness of a Voronoi cell (host seeds ng x 3 and table ng x ncoef): the
+    // per-node field, the grain ids and the grain tables the finest-level kernels read
+    void set_grains(CellRes* c, int ng, const double* seeds, const double* table);
+    // finest-level stiffness as a per-node field (host or device, ncoef x nn)
+    void set_field(CellRes* c, const void* C);
 
     // solve steps on the stream
     void begin(const std::vector<int>& cell_slots, const ae_solver_opts& o, double tol_rel, double tol_abs);

@@ -32,12 +32,37 @@ __device__ __forceinline__ const SCoef<R>& kfield(const CellLevelDev& L) {
     if constexpr (sizeof(R) == 8) return L.K64;
     else return L.K32;
 }
+template <class R>
+__device__ __forceinline__ const R* tabfield(const CellLevelDev& L) {
+    if constexpr (sizeof(R) == 8) return L.tab64;
+    else return L.tab32;
+}
+template <class R>
+__device__ __forceinline__ const R* itabfield(const CellLevelDev& L) {
+    if constexpr (sizeof(R) == 8) return L.itab64;
+    else return L.itab32;
+}
+
+// Which finest-level representation a launch serves: GR = true the grain tables (entries of
+// cells without them are skipped), GR = false the per-node arrays (on the finest level, entries
+// of cells with grain tables are skipped).  Coarser levels always use the per-node arrays.
+__device__ __forceinline__ bool rep_skips(bool GR, int m, const CellLevelDev& L) {
+    return GR ? (m != 0 || L.gid == nullptr) : (m == 0 && L.gid != nullptr);
+}
+
+// f = A u at node t of level m
+template <int M, class R, bool GR>
+__device__ __forceinline__ void level_apply(const CellLevelDev& L, int uniform, const R* U, int t, const POff& o,
+                                            R f[3]) {
+    if constexpr (GR) cell_apply_grains<M, R>(kfield<R>(L), uniform, L.gid, tabfield<R>(L), U, L.nn, t, o, f);
+    else cell_apply<M, R>(kfield<R>(L), uniform, cfield<R>(L), L.nn, U, L.nn, t, o, f);
+}
 
 constexpr int kCellThreads = 256;
 
 // one damped-Jacobi sweep of the correction at level m: from2 = 0 reads cor and writes cor2,
 // from2 = 1 the reverse.  ZERO: the input is the zero vector (the first sweep of a V-cycle).
-template <int M, class R, bool ZERO>
+template <int M, class R, bool ZERO, bool GR>
 __global__ void __launch_bounds__(kCellThreads) kb_smooth(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
                                                           int from2) {
     for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
@@ -45,34 +70,40 @@ __global__ void __launch_bounds__(kCellThreads) kb_smooth(CellArgs A, const Work
         const SolveDev& S = A.solves[w.id];
         if (m >= S.nlev - 1 || !S.st->active) continue;
         const CellLevelDev& L = A.cells[S.cell].lv[m];
+        if (rep_skips(GR, m, L)) continue;
         const int t = w.start + threadIdx.x;
         const int nn = L.nn;
         if (t >= nn) continue;
         const CellVec<R>& V = vec_of<R>(S, m);
         const R* __restrict__ xin = from2 ? V.cor2 : V.cor;
         R* __restrict__ xout = from2 ? V.cor : V.cor2;
-        const R* __restrict__ invD = ifield<R>(L);
         const R* __restrict__ b = V.res;
         const R omega = (R)A.omega;
+        // grain tables on the finest level of a Voronoi cell, per-node arrays otherwise
+        constexpr bool grains = GR;
+        const int g3 = grains ? 3 * (int)__ldg(L.gid + t) : 0;
+        const R* __restrict__ invD = grains ? itabfield<R>(L) + g3 : ifield<R>(L) + t;
+        const int ds = grains ? 1 : nn;  // component stride of invD / D
         if (ZERO) {
 #pragma unroll
-            for (int p = 0; p < 3; ++p) xout[p * nn + t] = (omega * b[p * nn + t]) * invD[p * nn + t];
+            for (int p = 0; p < 3; ++p) xout[p * nn + t] = (omega * b[p * nn + t]) * invD[p * ds];
             continue;
         }
         int i, j, k;
         cell_ijk(L.n, t, i, j, k);
         const POff o = cell_offsets(L.n, i, j, k);
         R f[3];
-        cell_apply<M, R>(kfield<R>(L), A.uniform, cfield<R>(L), nn, xin, nn, t, o, f);
+        level_apply<M, R, GR>(L, A.uniform, xin, t, o, f);
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
             const R xv = xin[p * nn + t];
             if constexpr (sizeof(R) == 8) {
                 // the reference's update, (1-w) x + w (b - (Ax - D x)) / D (Operator.cpp:154)
-                const R rx = f[p] - xv * L.D64[p * nn + t];
-                xout[p * nn + t] = (R(1) - omega) * xv + omega * (b[p * nn + t] - rx) * invD[p * nn + t];
+                const R Dv = grains ? L.dtab64[g3 + p] : L.D64[p * nn + t];
+                const R rx = f[p] - xv * Dv;
+                xout[p * nn + t] = (R(1) - omega) * xv + omega * (b[p * nn + t] - rx) * invD[p * ds];
             } else {
-                xout[p * nn + t] = xv + omega * (b[p * nn + t] - f[p]) * invD[p * nn + t];
+                xout[p * nn + t] = xv + omega * (b[p * nn + t] - f[p]) * invD[p * ds];
             }
         }
     }
@@ -95,7 +126,7 @@ __global__ void __launch_bounds__(kCellThreads) kb_copy2(CellArgs A, const Work*
 }
 
 // rescor = res - A cor at level m (inplace: into res)
-template <int M, class R>
+template <int M, class R, bool GR>
 __global__ void __launch_bounds__(kCellThreads) kb_rescor(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
                                                           int inplace) {
     for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
@@ -105,6 +136,7 @@ __global__ void __launch_bounds__(kCellThreads) kb_rescor(CellArgs A, const Work
         // (top level) also runs on single-level cells
         if ((!inplace && m >= S.nlev - 1) || !S.st->active) continue;
         const CellLevelDev& L = A.cells[S.cell].lv[m];
+        if (rep_skips(GR, m, L)) continue;
         const int t = w.start + threadIdx.x;
         const int nn = L.nn;
         if (t >= nn) continue;
@@ -113,7 +145,7 @@ __global__ void __launch_bounds__(kCellThreads) kb_rescor(CellArgs A, const Work
         cell_ijk(L.n, t, i, j, k);
         const POff o = cell_offsets(L.n, i, j, k);
         R f[3];
-        cell_apply<M, R>(kfield<R>(L), A.uniform, cfield<R>(L), nn, V.cor, nn, t, o, f);
+        level_apply<M, R, GR>(L, A.uniform, V.cor, t, o, f);
         R* out = inplace ? V.res : V.rescor;
 #pragma unroll
         for (int p = 0; p < 3; ++p) out[p * nn + t] = V.res[p * nn + t] - f[p];
@@ -306,13 +338,14 @@ __device__ __forceinline__ void block_partials(double (&v)[NQ], double* dst) {
 }
 
 // r = b - A x at level 0 with per-chunk sums of r (tab: one kRedChunk run per entry)
-template <int M>
+template <int M, bool GR>
 __global__ void __launch_bounds__(kCellThreads) kb_resid_top(CellArgs A, const Work* __restrict__ tab, int ntab) {
     for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
         const Work w = tab[e];
         const SolveDev& S = A.solves[w.id];
         if (!S.st->active) continue;
         const CellLevelDev& L = A.cells[S.cell].lv[0];
+        if (rep_skips(GR, 0, L)) continue;
         const int t = w.start + threadIdx.x;
         const int nn = L.nn;
         double v[3] = {0.0, 0.0, 0.0};
@@ -321,7 +354,7 @@ __global__ void __launch_bounds__(kCellThreads) kb_resid_top(CellArgs A, const W
             cell_ijk(L.n, t, i, j, k);
             const POff o = cell_offsets(L.n, i, j, k);
             double f[3];
-            cell_apply<M, double>(L.K64, A.uniform, L.C64, nn, S.x, nn, t, o, f);
+            level_apply<M, double, GR>(L, A.uniform, S.x, t, o, f);
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 v[p] = S.b[p * nn + t] - f[p];
@@ -628,7 +661,25 @@ __global__ void __launch_bounds__(kCellThreads) kb_grains(CellLevelDev L, double
         const double d = dx * dx + dy * dy + dz * dz;
         if (g == 0 || d < bd) { bd = d; best = g; }
     }
+    if (L.gid) L.gid[t] = (unsigned short)best;
     for (int q = 0; q < NC; ++q) L.C64[q * L.nn + t] = table[best * NC + q];
+}
+
+// per-grain FP32 stiffness, diagonal and 1/diagonal (the values kb_diag gives the grain's nodes)
+template <int M>
+__global__ void kb_grain_tables(CellLevelDev L) {
+    constexpr int NC = NCoef<M>::value;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= L.ngrains) return;
+    double d[3];
+    cell_diag<M, double>(L.K64, L.tab64 + g * NC, 1, 0, d);
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        L.dtab64[3 * g + p] = d[p];
+        L.itab64[3 * g + p] = 1.0 / d[p];
+        L.itab32[3 * g + p] = (float)(1.0 / d[p]);
+    }
+    for (int q = 0; q < NC; ++q) L.tab32[g * NC + q] = (float)L.tab64[g * NC + q];
 }
 
 inline int grid_of(int ntab, Shape sh) { return ntab < sh.grid ? ntab : sh.grid; }
@@ -642,18 +693,28 @@ void by_prec(int prec, F&& f) {
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
+// reps: bit 0 launch the per-node variant, bit 1 the grain-table variant (finest level)
+template <class F>
+void by_rep(int reps, F&& f) {
+    if (reps & 1) f(std::false_type());
+    if (reps & 2) f(std::true_type());
+}
+
 void cells_launch_smooth(int model, int prec, bool zero, const CellArgs& A, const Work* tab, int ntab, Shape sh,
-                         int m, int from2, cudaStream_t st) {
+                         int m, int from2, int reps, cudaStream_t st) {
     if (ntab == 0) return;
     dispatch_model<double>(model, [&](auto mm) {
         constexpr int M = decltype(mm)::value;
         by_prec(prec, [&](auto r) {
             using R = decltype(r);
-            if (zero) kb_smooth<M, R, true><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m, from2);
-            else kb_smooth<M, R, false><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m, from2);
+            by_rep(reps, [&](auto gr) {
+                constexpr bool GR = decltype(gr)::value;
+                if (zero) kb_smooth<M, R, true, GR><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m, from2);
+                else kb_smooth<M, R, false, GR><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m, from2);
+                launched();
+            });
         });
     });
-    launched();
 }
 void cells_launch_copy2(int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m, cudaStream_t st) {
     if (ntab == 0) return;
@@ -666,15 +727,18 @@ void cells_launch_fill0(int prec, const CellArgs& A, const Work* tab, int ntab, 
     launched();
 }
 void cells_launch_rescor(int model, int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m,
-                         int inplace, cudaStream_t st) {
+                         int inplace, int reps, cudaStream_t st) {
     if (ntab == 0) return;
     dispatch_model<double>(model, [&](auto mm) {
         constexpr int M = decltype(mm)::value;
         by_prec(prec, [&](auto r) {
-            kb_rescor<M, decltype(r)><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m, inplace);
+            by_rep(reps, [&](auto gr) {
+                kb_rescor<M, decltype(r), decltype(gr)::value><<<grid_of(ntab, sh), sh.chunk, 0, st>>>(A, tab, ntab, m,
+                                                                                                       inplace);
+                launched();
+            });
         });
     });
-    launched();
 }
 void cells_launch_restrict(int prec, const CellArgs& A, const Work* tab, int ntab, Shape sh, int m, cudaStream_t st) {
     if (ntab == 0) return;
@@ -697,12 +761,14 @@ void cells_launch_bottom(int model, int prec, const CellArgs& A, int nsolves, co
     });
     launched();
 }
-void cells_launch_resid_top(int model, const CellArgs& A, const Work* tab, int ntab, cudaStream_t st) {
+void cells_launch_resid_top(int model, const CellArgs& A, const Work* tab, int ntab, int reps, cudaStream_t st) {
     if (ntab == 0) return;
     dispatch_model<double>(model, [&](auto mm) {
-        kb_resid_top<decltype(mm)::value><<<ntab, kRedChunk, 0, st>>>(A, tab, ntab);
+        by_rep(reps, [&](auto gr) {
+            kb_resid_top<decltype(mm)::value, decltype(gr)::value><<<ntab, kRedChunk, 0, st>>>(A, tab, ntab);
+            launched();
+        });
     });
-    launched();
 }
 void cells_launch_rhs(int model, const CellArgs& A, const Work* tab, int ntab, cudaStream_t st) {
     if (ntab == 0) return;
@@ -766,6 +832,12 @@ void cells_launch_grains(int model, const CellLevelDev& L, const double len[3], 
             L, len[0], len[1], len[2], seeds, ng, table);
     });
     launched();
+    if (L.gid && L.ngrains > 0) {
+        dispatch_model<double>(model, [&](auto mm) {
+            kb_grain_tables<decltype(mm)::value><<<(L.ngrains + 127) / 128, 128, 0, st>>>(L);
+        });
+        launched();
+    }
 }
 void cells_launch_diag(int model, const CellArgs& A, const Work* tab, int ntab, int m, int* nan_flag,
                        cudaStream_t st) {

@@ -182,6 +182,14 @@ __device__ __forceinline__ void div_of(const R* a, const R b[3][3][3], R f[3]) {
 
 // read-only load: through the non-coherent cache for global memory (LDG), plain otherwise
 // (stiffness staged in shared memory)
+// A Voronoi stiffness on one level: a grain id per node (laid out like the level's stiffness
+// view) and a per-grain coefficient table tab[g * ncoef + q].  gid == nullptr: not used.
+template <class R>
+struct Grains {
+    const unsigned short* gid = nullptr;
+    const R* tab = nullptr;
+};
+
 template <bool LDG, class T>
 __device__ __forceinline__ T ldv(const T* p) {
     if constexpr (LDG) return __ldg(p);
@@ -394,6 +402,99 @@ __device__ __forceinline__ void apply_node(const Geo& g, const SCoef<R>& K, cons
         gradC_col<M, R, LDG>(C, cs, cc, csz, gu, 2, c2);
 #pragma unroll
         for (int r = 0; r < 3; ++r) f[r] += (c0[r] * K.h[0] + c1[r] * K.h[1]) + c2[r] * K.h[2];
+    }
+}
+
+// apply_node for a stiffness given as a grain id per node (gid, strides gsy, gsz, node index gc)
+// and a per-grain coefficient table (tab[g * ncoef + q]): the same arithmetic on the same values.
+// A direction whose two neighbours lie in one grain has an exactly zero stiffness difference; its
+// grad C column is zero and its table reads are skipped.
+template <int M, class R>
+__device__ __forceinline__ void apply_node_grains(const Geo& g, const SCoef<R>& K, const BCP& bc, bool uniform,
+                                                  const unsigned short* __restrict__ gid, long long gc,
+                                                  long long gsy, long long gsz, const R* __restrict__ tab,
+                                                  const R* __restrict__ U, long long usc, long long uc, long long usy,
+                                                  long long usz, int i, int j, int k, R f[3]) {
+    constexpr int NC = NCoef<M>::value;
+    const R* a0 = tab + (int)__ldg(gid + gc) * NC;
+    R nrm[3];
+    const int face = classify<R>(g, i, j, k, nrm);
+    if (face >= 0) {
+        const int ci[3] = {i, j, k};
+        const long long os[3] = {1, usy, usz};
+        R gu[3][3], u[3];
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            const R* up = U + p * usc + uc;
+            u[p] = up[0];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const long long o = os[d];
+                if (ci[d] == g.dlo[d]) gu[p][d] = (up[o] - up[0]) * K.id[d];
+                else if (ci[d] == g.dhi[d]) gu[p][d] = (up[0] - up[-o]) * K.id[d];
+                else gu[p][d] = (up[o] - up[-o]) * K.h[d];
+            }
+        }
+        const unsigned char* t = bc.t[face];
+        R s[3][3];
+        bool need_s = (t[0] == TRAC) || (t[1] == TRAC) || (t[2] == TRAC);
+        if (need_s) {
+            R a[NC];
+#pragma unroll
+            for (int q = 0; q < NC; ++q) a[q] = __ldg(a0 + q);
+            stress_of<M, R>(a, gu, s);
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            R v = R(0);
+            if (t[r] == DISP) v = u[r];
+            else if (t[r] == TRAC) v = s[r][0] * nrm[0] + s[r][1] * nrm[1] + s[r][2] * nrm[2];
+            else if (t[r] == NEUMANN) v = gu[r][0] * nrm[0] + gu[r][1] * nrm[1] + gu[r][2] * nrm[2];
+            f[r] = v;
+        }
+        return;
+    }
+    R gu[3][3], b[3][3][3];
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const R* up = U + p * usc + uc;
+        const R c0 = up[0];
+        const R xm = up[-1], xp = up[1], ym = up[-usy], yp = up[usy], zm = up[-usz], zp = up[usz];
+        gu[p][0] = (xp - xm) * K.h[0];
+        gu[p][1] = (yp - ym) * K.h[1];
+        gu[p][2] = (zp - zm) * K.h[2];
+        b[p][0][0] = (xp - R(2) * c0 + xm) * K.i2[0];
+        b[p][1][1] = (yp - R(2) * c0 + ym) * K.i2[1];
+        b[p][2][2] = (zp - R(2) * c0 + zm) * K.i2[2];
+        b[p][0][1] = (up[1 + usy] + up[-1 - usy] - up[1 - usy] - up[-1 + usy]) * K.m01;
+        b[p][0][2] = (up[1 + usz] + up[-1 - usz] - up[1 - usz] - up[-1 + usz]) * K.m02;
+        b[p][1][2] = (up[usy + usz] + up[-usy - usz] - up[usy - usz] - up[-usy + usz]) * K.m12;
+        b[p][1][0] = b[p][0][1];
+        b[p][2][0] = b[p][0][2];
+        b[p][2][1] = b[p][1][2];
+    }
+    {
+        R a[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) a[q] = __ldg(a0 + q);
+        div_of<M, R>(a, b, f);
+    }
+    if (!uniform) {
+        const long long go[3] = {1, gsy, gsz};
+        R col[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int gp = __ldg(gid + gc + go[d]), gm = __ldg(gid + gc - go[d]);
+            if (gp == gm) {
+                col[d][0] = col[d][1] = col[d][2] = R(0);
+            } else {
+                const R* cp = tab + gp * NC;
+                const R* cm = tab + gm * NC;
+                gradC_col_f<M, R>([&](int q) { return __ldg(cp + q) - __ldg(cm + q); }, gu, d, col[d]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) f[r] += (col[0][r] * K.h[0] + col[1][r] * K.h[1]) + col[2][r] * K.h[2];
     }
 }
 

@@ -73,17 +73,30 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* o
     }
 }
 
+// f = A u at one node: through the grain tables when the level has them (G.gid laid out like C),
+// otherwise through the per-node stiffness C
+// (GR: compiled for the grain tables, so each variant keeps its own register budget)
+template <int M, class R, bool GR>
+__device__ __forceinline__ void apply_any(const OpParams& P, const SCoef<R>& K, const View<const R>& C,
+                                          const Grains<R>& G, const View<const R>& u, int i, int j, int k, R v[3]) {
+    if constexpr (GR)
+        apply_node_grains<M, R>(P.g, K, P.bc, P.uniform, G.gid, C.at(i, j, k), C.sy, C.sz, G.tab, u.p, u.sc,
+                                u.at(i, j, k), u.sy, u.sz, i, j, k, v);
+    else
+        apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, u.p, u.sc, u.at(i, j, k),
+                         u.sy, u.sz, i, j, k, v);
+}
+
 // ------------------------------------------------------------------ Fapply
-template <int M, class R>
-__global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg reg, View<const R> C, View<const R> u,
-                                                   View<R> f) {
+template <int M, class R, bool GR>
+__global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
+                                                   View<const R> u, View<R> f) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= reg.n) return;
     int i, j, k;
     reg_ijk(reg, t, i, j, k);
     R v[3];
-    apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, u.p, u.sc, u.at(i, j, k), u.sy,
-                     u.sz, i, j, k, v);
+    apply_any<M, R, GR>(P, K, C, G, u, i, j, k, v);
     const long long o = f.at(i, j, k);
     f.p[o] = v[0];
     f.p[o + f.sc] = v[1];
@@ -91,8 +104,8 @@ __global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg r
 }
 
 // ------------------------------------------------------------------ residual (+ norm, + FP32 copy)
-template <int M, class R, bool NORM, bool R32>
-__global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg reg, View<const R> C,
+template <int M, class R, bool NORM, bool R32, bool GR>
+__global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
                                                      View<const R> x, View<const R> b, View<R> r,
                                                      unsigned long long* norm, View<float> r32) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -101,8 +114,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg
         int i, j, k;
         reg_ijk(reg, t, i, j, k);
         R v[3];
-        apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, x.p, x.sc, x.at(i, j, k),
-                         x.sy, x.sz, i, j, k, v);
+        apply_any<M, R, GR>(P, K, C, G, x, i, j, k, v);
         const long long ob = b.at(i, j, k), orr = r.at(i, j, k);
         const bool inv = in_box(P.g.vlo, P.g.vhi, i, j, k);
 #pragma unroll
@@ -119,8 +131,8 @@ __global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg
 
 // ------------------------------------------------------------------ damped Jacobi sweep
 // src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in.
-template <int M, class R>
-__global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg reg, View<const R> C,
+template <int M, class R, bool GR>
+__global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
                                                    View<const R> invD, View<const R> D, View<const R> xi,
                                                    View<const R> b, View<R> xo, R omega) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,8 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg r
         return;
     }
     R v[3];
-    apply_node<M, R>(g, K, P.bc, P.uniform, C.p, C.sc, C.at(i, j, k), C.sy, C.sz, xi.p, xi.sc, ox, xi.sy, xi.sz, i,
-                     j, k, v);
+    apply_any<M, R, GR>(P, K, C, G, xi, i, j, k, v);
     const long long od = invD.at(i, j, k), ob = b.at(i, j, k);
 #pragma unroll
     for (int n = 0; n < 3; ++n) {

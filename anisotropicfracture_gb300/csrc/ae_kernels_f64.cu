@@ -46,6 +46,38 @@ void launch_bc_init(const Geo& g, const BCP& bc, const double* val, int homogene
     launched();
 }
 
+// ------------------------------------------------------------------ Voronoi stiffness
+__global__ void __launch_bounds__(kBlock) k_grains_box(Reg reg, View<const int> ids, View<unsigned short> gid,
+                                                       View<double> C, const double* __restrict__ tab, int ng, int nc,
+                                                       int* bad) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const int id = ids.p[ids.at(i, j, k)];
+    if (id < 0 || id >= ng) {
+        atomicExch(bad, 1);
+        return;
+    }
+    gid.p[gid.at(i, j, k)] = (unsigned short)id;
+    const long long o = C.at(i, j, k);
+    for (int q = 0; q < nc; ++q) C.p[o + q * C.sc] = tab[id * nc + q];
+}
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) b[t] = (float)a[t];
+}
+void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned short> gid, View<double> C,
+                       const double* tab, int ng, int nc, float* tab32, int* bad, cudaStream_t st) {
+    const Reg reg = make_reg(region);
+    if (reg.n > 0) {
+        k_grains_box<<<nblocks(reg.n), kBlock, 0, st>>>(reg, ids, gid, C, tab, ng, nc, bad);
+        launched();
+    }
+    k_to_float<<<(ng * nc + 255) / 256, 256, 0, st>>>(tab, tab32, ng * nc);
+    launched();
+}
+
 // ------------------------------------------------------------------ Strain / Stress / Energy
 // src/Operator/Elastic.cpp:399-572 (valid box, boundary-aware first derivatives)
 __device__ __forceinline__ void grad_at(const Geo& g, const SCoef<double>& K, const View<const double>& u, int i,

@@ -97,19 +97,22 @@ struct OpParams {
 };
 
 // ------------------------------------------------------------------ launchers
+// G: the level's grain ids (laid out like C) and per-grain table, when the stiffness was given
+// as a Voronoi map; the kernels then read those instead of C (same values).
 template <class R>
-void launch_fapply(const OpParams& P, View<const R> C, View<const R> u, View<R> f, cudaStream_t st);
+void launch_fapply(const OpParams& P, View<const R> C, View<const R> u, View<R> f, cudaStream_t st,
+                   Grains<R> G = Grains<R>{});
 // r = b - A x over the apply region; if norm != nullptr, atomically max-reduce |r| over
 // valid ∩ domain into *norm (bit pattern of a non-negative double, zero it first);
 // if r32 != nullptr also store (float) r there.
 template <class R>
 void launch_residual(const OpParams& P, View<const R> C, View<const R> x, View<const R> b, View<R> r,
-                     unsigned long long* norm, View<float>* r32, cudaStream_t st);
+                     unsigned long long* norm, View<float>* r32, cudaStream_t st, Grains<R> G = Grains<R>{});
 // One damped-Jacobi sweep: xo = (1-w) xi + w (b - (A xi - D xi)) / D on grow(valid,1)∩dom,
 // zero on the ring grow(valid,2) \ grow(valid,1), copy elsewhere.
 template <class R>
 void launch_jacobi(const OpParams& P, View<const R> C, View<const R> invD, View<const R> D, View<const R> xi,
-                   View<const R> b, View<R> xo, R omega, cudaStream_t st);
+                   View<const R> b, View<R> xo, R omega, cudaStream_t st, Grains<R> G = Grains<R>{});
 // Fapply (op 0), damped-Jacobi sweep (op 1) or residual (op 2) with the z-marching tiled
 // kernel, on the level's internal storage views only.  tiled_init must have run once.
 template <class R>
@@ -148,6 +151,11 @@ void launch_strain(const Geo& g, View<const double> u, View<double> e, int voigt
 void launch_stress(const OpParams& P, View<const double> C, View<const double> u, View<double> s, int voigt,
                    cudaStream_t st);
 void launch_energy(const OpParams& P, View<const double> C, View<const double> u, View<double> w, cudaStream_t st);
+
+// Voronoi stiffness over `region`: ids (int32 per node) -> gid (uint16) and the per-node FP64
+// stiffness C = tab[id]; tab32 = (float) tab.  *bad is set if an id is outside [0, ng).
+void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned short> gid, View<double> C,
+                       const double* tab, int ng, int nc, float* tab32, int* bad, cudaStream_t st);
 
 struct BottomArgs {
     OpParams P;

@@ -145,24 +145,11 @@ void ae_server_s::run() {
                         c->tag = r->ticket;
                         r->cell = c;
                         for (int k = 0; k < r->desc.nrhs; ++k) c->E[k] = r->E[k];
-                        if (r->ngrains > 0) {
-                            const size_t ns = sizeof(double) * r->seeds.size(), nt = sizeof(double) * r->table.size();
-                            void* buf = nullptr;
-                            AEH_CHECK(cudaMallocAsync(&buf, ns + nt, E.st));
-                            AEH_CHECK(cudaMemcpyAsync(buf, r->seeds.data(), ns, cudaMemcpyHostToDevice, E.st));
-                            AEH_CHECK(
-                                cudaMemcpyAsync((char*)buf + ns, r->table.data(), nt, cudaMemcpyHostToDevice, E.st));
-                            cells_launch_grains(E.model, c->lv[0], c->len, (const double*)buf, r->ngrains,
-                                                (const double*)((char*)buf + ns), E.st);
-                            AEH_CHECK(cudaFreeAsync(buf, E.st));
-                        } else {
-                            AEH_CHECK(cudaMemcpyAsync(c->lv[0].C64, r->field.data(), sizeof(double) * r->field.size(),
-                                                      cudaMemcpyHostToDevice, E.st));
-                        }
-                        AEH_CHECK(cudaStreamSynchronize(E.st));  // the host inputs may be released now
+                        // both synchronise the stream: the host inputs may be released afterwards
+                        if (r->ngrains > 0) E.set_grains(c, r->ngrains, r->seeds.data(), r->table.data());
+                        else E.set_field(c, r->field.data());
                         r->field.clear();
                         r->field.shrink_to_fit();
-                        c->model_set = true;
                         E.live.push_back(c);
                         ok.push_back(r);
                     } catch (const hx::CudaErr& e) {

@@ -161,6 +161,20 @@ class Elastic:
             f = coeffs.fab()
             check(load().ae_op_set_model(self._h, int(a), C.byref(f)))
 
+    def SetModelGrains(self, a, grain_id, table):
+        """SetModel(amrlev, ...) for a Voronoi stiffness: grain_id a Field of int32 ids (ncomp 1),
+        table (ngrains, ncoef); equivalent to SetModel with C = table[grain_id]."""
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        arr = grain_id.arr
+        if isinstance(arr, np.ndarray):
+            if arr.dtype != np.int32:
+                raise TypeError("grain ids must be int32")
+        elif str(arr.dtype) != "torch.int32":
+            raise TypeError("grain ids must be int32")
+        f = grain_id.fab()
+        f.is_float = 0
+        check(load().ae_op_set_model_grains(self._h, int(a), C.byref(f), table.shape[0], table.ctypes.data))
+
     def SetBC(self, bc):
         self.m_bc = bc
         t = np.ascontiguousarray(bc.type, dtype=np.int32)

@@ -44,6 +44,11 @@ L2_BYTES = 129 * 2 ** 20
 # FP32 fused Jacobi sweep, cubic 21-coefficient stiffness: x in 12 + b 12 + diag 12 + C 84 + x out 12
 JACOBI32_BYTES_PER_NODE = 132
 FAPPLY64_BYTES_PER_NODE = 216
+FAPPLY32_BYTES_PER_NODE = 108
+# the same kernels on a grain map: stiffness 2 B per node (uint16 grain id) instead of 84 / 168
+JACOBI32_BYTES_PER_NODE_GRAINS = 12 + 12 + 12 + 2 + 12
+FAPPLY64_BYTES_PER_NODE_GRAINS = 24 + 2 + 24
+FAPPLY32_BYTES_PER_NODE_GRAINS = 12 + 2 + 12
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
 # time to a full solve in the reference arm, which cannot afford a full CPU solve.
@@ -74,8 +79,8 @@ def workload(n=256, nseeds=64, seed_points=1, seed_rot=2):
         hi = [L["hi"] + L["ng"]] * 3
         gid = microstructure.voronoi_grain_ids(lo, hi, (dx, dx, dx), seeds)
         Cf = np.ascontiguousarray(np.moveaxis(table[gid].astype(np.float64), -1, 0))
-        del gid
-        out.append(dict(L, dx=dx, store_lo=lo, store_hi=hi, C=Cf))
+        out.append(dict(L, dx=dx, store_lo=lo, store_hi=hi, C=Cf, gid=np.ascontiguousarray(gid[None].astype(np.int32)),
+                        table=table))
     return out, bc
 
 
@@ -409,6 +414,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--inner", type=int, default=int(os.environ.get("AE_INNER_CYCLES", "8")),
                     help="FP32 cycles per FP64 residual in mixed precision")
+    ap.add_argument("--per-node-model", action="store_true",
+                    help="give the single-box stiffness per node (ae_op_set_model) instead of as grain ids + table")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cell workload")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-cell workload")
     ap.add_argument("--only-cells", action="store_true", help="run only the batched/served cell workloads")
@@ -446,7 +453,10 @@ def main():
     descs = [level_desc(L["cells"], lo=(L["lo"],) * 3, hi=(L["hi"],) * 3) for L in levels]
     op = Elastic(descs, models.MAJORMINOR)
     for a, L in enumerate(levels):
-        op.SetModel(a, Field(L["C"], tuple(L["store_lo"])))
+        if args.per_node_model:
+            op.SetModel(a, Field(L["C"], tuple(L["store_lo"])))
+        else:  # the Voronoi map itself: grain ids + per-grain table (same values, 2 B per node)
+            op.SetModelGrains(a, Field(L["gid"], tuple(L["store_lo"])), L["table"])
     op.SetBC(bc)
     op.SetUniform(False)
     op.prepareForSolve()
@@ -551,9 +561,15 @@ def main():
     _lib.check(lib.ae_profile_kernel(op.handle, 0, 0, 0, 1, 20, C.byref(ms_f32)))
     n0 = int(np.prod(rhs_h[0].shape[1:]))
     peak, peak_kind = measured_peaks()
-    jac_gbs = JACOBI32_BYTES_PER_NODE * n0 / (ms_jac.value * 1e-3) / 1e9
-    fapply64_gbs = FAPPLY64_BYTES_PER_NODE * n0 / (ms_f64.value * 1e-3) / 1e9
-    fapply32_gbs = 108 * n0 / (ms_f32.value * 1e-3) / 1e9
+    # bytes per node the kernels must move: per-node stiffness (canonical figures) or the grain
+    # map (2-byte id per node; the per-grain table stays in L1/L2)
+    grains = not args.per_node_model
+    b_jac = JACOBI32_BYTES_PER_NODE_GRAINS if grains else JACOBI32_BYTES_PER_NODE
+    b_f64 = FAPPLY64_BYTES_PER_NODE_GRAINS if grains else FAPPLY64_BYTES_PER_NODE
+    b_f32 = FAPPLY32_BYTES_PER_NODE_GRAINS if grains else FAPPLY32_BYTES_PER_NODE
+    jac_gbs = b_jac * n0 / (ms_jac.value * 1e-3) / 1e9
+    fapply64_gbs = b_f64 * n0 / (ms_f64.value * 1e-3) / 1e9
+    fapply32_gbs = b_f32 * n0 / (ms_f32.value * 1e-3) / 1e9
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -572,6 +588,8 @@ def main():
                                "(2 x 257^3 nodes), cubic 1.68/1.21/0.75, 64 Voronoi grains",
                    "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, CG bottom", "tol_rel": 1e-8,
                    "precision": "mixed: FP32 cycle in FP64 refinement", "inner_cycles": args.inner,
+                   "stiffness": ("per-node coefficients (ae_op_set_model)" if args.per_node_model else
+                                 "Voronoi grain ids + per-grain table (ae_op_set_model_grains)"),
                    "nodes": nodes,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (stiffness %.1f GB)" % (sum(L["C"].nbytes for L in levels) / 1e9)},
@@ -585,10 +603,14 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "FP32 fused Jacobi sweep (cubic), coarse level 257^3",
                      "achieved": jac_gbs, "peak": peak, "unit": "GB/s", "frac": jac_gbs / peak,
                      "peak_kind": peak_kind, "traffic": None,
-                     "bytes_per_node": JACOBI32_BYTES_PER_NODE, "ms_per_launch": ms_jac.value},
+                     "bytes_per_node": b_jac, "ms_per_launch": ms_jac.value,
+                     "stiffness": "grain ids + table" if grains else "per node",
+                     "canonical_bytes_per_node": JACOBI32_BYTES_PER_NODE,
+                     "canonical_gbs": JACOBI32_BYTES_PER_NODE * n0 / (ms_jac.value * 1e-3) / 1e9},
         "fapply": {"fp64_gbs": fapply64_gbs, "fp64_ms": ms_f64.value, "fp32_gbs": fapply32_gbs,
-                   "fp32_ms": ms_f32.value, "bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
-                   "bytes_per_node_fp32": 108},
+                   "fp32_ms": ms_f32.value, "bytes_per_node_fp64": b_f64, "bytes_per_node_fp32": b_f32,
+                   "canonical_bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
+                   "canonical_bytes_per_node_fp32": FAPPLY32_BYTES_PER_NODE},
         "clocks": clk,
         "gpu_launches": int(launches),
         "cpu_baseline": cpu,

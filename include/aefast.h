@@ -126,6 +126,13 @@ int ae_op_set_stream(ae_op* op, void* stream);
 int ae_op_set_model(ae_op* op, int amrlev, const ae_fab* coeffs);
 /* Operator::Elastic<T>::SetModel(T&) (Elastic.cpp:57-82): one stiffness on every node. */
 int ae_op_set_model_uniform(ae_op* op, const double* coeffs, int ncoef);
+/* SetModel for a stiffness that takes one of `ngrains` values per node, as a Voronoi
+ * polycrystal does (IC::Voronoi, src/IC/Voronoi.H:47-101, one Linear::Cubic per grain): grain_id
+ * is an int32 fab (ncomp 1) over the same region as ae_op_set_model's, table is ngrains x ncoef
+ * (host or device).  Equivalent to ae_op_set_model with C(x) = table[grain_id(x)]; the sweeps on
+ * the level then read 2-byte grain ids and the table instead of 84/168 bytes per node, with the
+ * same arithmetic on the same values. */
+int ae_op_set_model_grains(ae_op* op, int amrlev, const ae_fab* grain_id, int ngrains, const double* table);
 /* BC::Operator::Elastic<T>::Set for all 26 faces (Elastic.H:61-69); val used by ae_bc_init. */
 int ae_op_set_bc(ae_op* op, const int* type /*[26][3]*/, const double* val /*[26][3]*/);
 /* Operator::Elastic<T>::SetUniform / SetHomogeneous (Elastic.H:48,111). */
