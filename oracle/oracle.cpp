@@ -87,6 +87,13 @@ inline double Dmix(const double* f, long oa, long ob, double dxa, double dxb) {
     return 0.25 * (f[oa + ob] + f[-oa - ob] - f[oa - ob] - f[-oa + ob]) / (dxa * dxb);
 }
 
+// max(m, |v|) for residual max-norms; a NaN makes the norm infinite (std::max alone would drop
+// it and report a diverged solve as converged)
+inline double amax(double m, double v) {
+    const double a = std::fabs(v);
+    return (a != a) ? INFINITY : std::max(m, a);
+}
+
 // ---------------------------------------------------------------- Set::Matrix4 contractions
 int ncoef_of(int model) { return model == ORC_ISOTROPIC ? 2 : model == ORC_MAJORMINOR ? 21 : 9; }
 
@@ -374,7 +381,7 @@ double residual(const Lev& L, int model, const double* C, const int* bctype, int
     for (int n = 0; n < 3; ++n)
         for (int k = v.lo[2]; k <= v.hi[2]; ++k)
             for (int j = v.lo[1]; j <= v.hi[1]; ++j)
-                for (int i = v.lo[0]; i <= v.hi[0]; ++i) mx = std::max(mx, std::fabs(R[n * L.nn + L.at(i, j, k)]));
+                for (int i = v.lo[0]; i <= v.hi[0]; ++i) mx = amax(mx, R[n * L.nn + L.at(i, j, k)]);
     return mx;
 }
 
@@ -698,7 +705,7 @@ struct Amr {
         for (int n = 0; n < 3; ++n)
             for (int k = r.lo[2]; k <= r.hi[2]; ++k)
                 for (int j = r.lo[1]; j <= r.hi[1]; ++j)
-                    for (int i = r.lo[0]; i <= r.hi[0]; ++i) m = std::max(m, std::fabs(v[n * l.nn + l.at(i, j, k)]));
+                    for (int i = r.lo[0]; i <= r.hi[0]; ++i) m = amax(m, v[n * l.nn + l.at(i, j, k)]);
         return m;
     }
     // MLMG::computeMLResidual + composite max-norm
@@ -1029,7 +1036,7 @@ int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const*
         rn = A.ml_residual();
         if (stats && it < 256) stats->hist[it] = rn;
         iters = it + 1;
-        if (!(rn == rn)) break;
+        if (!std::isfinite(rn)) break;
         if (rn <= target) conv = 1;
     }
     if (stats) {
@@ -1219,7 +1226,7 @@ void psubtract(const PLev& L, double* v, const double m[3]) {
 }
 double pninf(const PLev& L, const double* v) {
     double m = 0.0;
-    for (long c = 0; c < 3 * L.nn; ++c) m = std::max(m, std::fabs(v[c]));
+    for (long c = 0; c < 3 * L.nn; ++c) m = amax(m, v[c]);
     return m;
 }
 
@@ -1572,7 +1579,7 @@ int orc_rve_solve(const orc_rve_level* L0, int model, const double* C, const dou
         rn = presidual(L, model, S.lv[0].C.data(), S.uniform, w, b.data(), res0v, 1, mu);
         if (stats && it < 256) stats->hist[it] = rn;
         iters = it + 1;
-        if (!(rn == rn)) break;
+        if (!std::isfinite(rn)) break;
         if (rn <= target) conv = 1;
     }
     double wm[3];

@@ -60,21 +60,28 @@ def test_grain_kernels_equal_per_node_kernels(precision):
     bc = bc_random(rng)
     a, b = _ops(Ls, bc, gids, Cs, tab)
     dt = np.float64 if precision == "fp64" else np.float32
-    u = rng.standard_normal((3,) + Ls[0].shape).astype(dt)
-    rhs = rng.standard_normal((3,) + Ls[0].shape).astype(dt)
-    fa, fb = np.zeros_like(u), np.zeros_like(u)
+
+    def dev(x):
+        return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+    u = dev(rng.standard_normal((3,) + Ls[0].shape).astype(dt))
+    rhs = dev(rng.standard_normal((3,) + Ls[0].shape).astype(dt))
+    fa, fb = torch.zeros_like(u), torch.zeros_like(u)
     a.Fapply(0, 0, Field(fa), Field(u))
     b.Fapply(0, 0, Field(fb), Field(u))
-    assert np.array_equal(fa, fb)
+    torch.cuda.synchronize()
+    assert torch.equal(fa, fb)
     if precision == "fp64":
-        ra, rb = np.zeros_like(u), np.zeros_like(u)
+        ra, rb = torch.zeros_like(u), torch.zeros_like(u)
         na = a.Residual(0, 0, Field(ra), Field(u), Field(rhs))
         nb = b.Residual(0, 0, Field(rb), Field(u), Field(rhs))
-        assert np.array_equal(ra, rb) and na == nb
-        xa, xb = u.copy(), u.copy()
+        torch.cuda.synchronize()
+        assert torch.equal(ra, rb) and na == nb
+        xa, xb = u.clone(), u.clone()
         a.Fsmooth(0, 0, Field(xa), Field(rhs))
         b.Fsmooth(0, 0, Field(xb), Field(rhs))
-        assert np.array_equal(xa, xb)
+        torch.cuda.synchronize()
+        assert torch.equal(xa, xb)
     a.close()
     b.close()
 
