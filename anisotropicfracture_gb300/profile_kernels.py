@@ -19,6 +19,8 @@ KERNELS = {"fapply": 0, "jacobi": 1, "residual": 2, "restrict": 3, "interp": 4}
 # canonical algorithmic bytes per (fine) node, cubic stiffness: {precision: bytes}
 BYTES = {"fapply": {8: 216, 4: 108}, "jacobi": {8: 264, 4: 132}, "residual": {8: 240, 4: 120},
          "restrict": {8: 27, 4: 13.5}, "interp": {8: 51, 4: 25.5}}
+# the same kernels on a grain map: the stiffness is a 2-byte id per node
+GRAIN_BYTES = {"fapply": {8: 50, 4: 26}, "jacobi": {8: 122, 4: 50}, "residual": {8: 74, 4: 38}}
 
 
 def main(argv=None):
@@ -29,6 +31,8 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--mglev", type=int, default=0)
     ap.add_argument("--grains", type=int, default=64)
+    ap.add_argument("--grain-map", action="store_true",
+                    help="give the stiffness as grain ids + table (ae_op_set_model_grains)")
     args = ap.parse_args(argv)
 
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -38,9 +42,12 @@ def main(argv=None):
     from anisotropicfracture_gb300.elastic import BCElastic, Elastic, Field, level_desc
 
     n = args.cells
-    Cf, _, _ = microstructure.cubic_polycrystal((0, 0, 0), (n, n, n), (1.0 / n,) * 3, nseeds=args.grains)
+    Cf, gid, table = microstructure.cubic_polycrystal((0, 0, 0), (n, n, n), (1.0 / n,) * 3, nseeds=args.grains)
     op = Elastic([level_desc(n)], models.MAJORMINOR)
-    op.SetModel(0, Field(Cf))
+    if args.grain_map:
+        op.SetModelGrains(0, Field(np.ascontiguousarray(gid[None].astype(np.int32))), table)
+    else:
+        op.SetModel(0, Field(Cf))
     bc = BCElastic()
     for f in ["XLO", "XHI", "YLO", "YHI", "XLO_YLO", "XLO_YHI", "XHI_YLO", "XHI_YHI"]:
         for d in range(3):
@@ -53,9 +60,11 @@ def main(argv=None):
     ms = C.c_double(0.0)
     _lib.check(lib.ae_profile_kernel(op.handle, KERNELS[args.kernel], 0, args.mglev, prec, args.reps, C.byref(ms)))
     nodes = (n // 2 ** args.mglev + 1) ** 3
-    nbytes = BYTES[args.kernel][4 if prec else 8] * nodes
+    table = GRAIN_BYTES if (args.grain_map and args.mglev == 0 and args.kernel in GRAIN_BYTES) else BYTES
+    nbytes = table[args.kernel][4 if prec else 8] * nodes
     print(json.dumps({"kernel": args.kernel, "precision": args.precision, "cells": n, "mglev": args.mglev,
-                      "nodes": nodes, "ms_per_launch": ms.value,
+                      "grain_map": bool(args.grain_map), "nodes": nodes, "ms_per_launch": ms.value,
+                      "bytes_per_node": table[args.kernel][4 if prec else 8],
                       "algorithmic_GBps": nbytes / (ms.value * 1e-3) / 1e9}))
     op.close()
 

@@ -49,6 +49,7 @@ def _ops(Ls, bc, gids, Cs, tab):
     for op in (a, b):
         op.SetBC(bc)
         op.SetUniform(False)
+        op.prepareForSolve()
     return a, b
 
 
