@@ -120,6 +120,8 @@ struct ae_op_s {
     unsigned long long* hnorm = nullptr;  // pinned mirror
     int* dflag = nullptr;                 // [0] NaN/zero-diagonal flags, [1] bottom failures
     double* bottom_work = nullptr;
+    double* newton_dw = nullptr;  // Newton<T> scratch: 9 components over the largest level store
+    long long newton_dw_n = 0;
     long long bottom_work_n = 0;
     bool prepared = false;
     bool have32 = false;
@@ -1183,6 +1185,79 @@ int ae_stress(ae_op* op, int amrlev, const ae_fab* sig, const ae_fab* u, int voi
         require(is_device_ptr(u->data) && is_device_ptr(sig->data), "Stress: fabs must be device memory");
         launch_stress(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
                       fab_view<double>(*sig), voigt, op->st);
+    });
+}
+
+int ae_newton_residual(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, const ae_fab* F0, ae_fab* rhs) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(op->bc_set, "SetBC has not been called", AE_ERR_STATE);
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        require(op->amr[amrlev].model_set, "SetModel has not been called on this level", AE_ERR_STATE);
+        const Box3 bx2 = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        const Box3 bx1 = box_isect(box_isect(box_grow(geo_valid(L.g), 1), geo_domain(L.g)), geo_store(L.g));
+        check_fab(u, bx2, 3, "NewtonResidual u");
+        check_fab(b, bx1, 3, "NewtonResidual b");
+        check_fab(rhs, bx1, 3, "NewtonResidual rhs");
+        if (F0) check_fab(F0, bx2, 9, "NewtonResidual F0");
+        require(!u->is_float && !b->is_float && !rhs->is_float && (!F0 || !F0->is_float),
+                "NewtonResidual: FP64 fields required");
+        if (op->newton_dw_n < 9 * L.nn) {
+            op->newton_dw = op->alloc<double>(9 * L.nn);
+            op->newton_dw_n = 9 * L.nn;
+        }
+        // host fabs are staged through temporary device copies (rhs is copied back)
+        std::vector<void*> tmp;
+        auto on_device = [&](const ae_fab* f, bool copy_in) -> ae_fab {
+            ae_fab d = *f;
+            if (is_device_ptr(f->data)) return d;
+            const size_t bytes = sizeof(double) * (size_t)fab_elems(*f);
+            void* p = nullptr;
+            AE_CHECK(cudaMalloc(&p, bytes));
+            tmp.push_back(p);
+            if (copy_in) AE_CHECK(cudaMemcpyAsync(p, f->data, bytes, cudaMemcpyHostToDevice, op->st));
+            d.data = p;
+            return d;
+        };
+        struct Free {
+            std::vector<void*>& v;
+            ~Free() { for (void* p : v) cudaFree(p); }
+        } free_{tmp};
+        const ae_fab ud = on_device(u, true), bd = on_device(b, true), rd = on_device(rhs, true);
+        ae_fab fd{};
+        if (F0) fd = on_device(F0, true);
+        launch_newton_residual(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(ud)),
+                               cview(fab_view<double>(bd)), F0 ? cview(fab_view<double>(fd)) : View<const double>{},
+                               level_view(L.g, op->newton_dw), fab_view<double>(rd), op->st);
+        if (rd.data != rhs->data)
+            AE_CHECK(cudaMemcpyAsync(rhs->data, rd.data, sizeof(double) * (size_t)fab_elems(*rhs),
+                                     cudaMemcpyDeviceToHost, op->st));
+        if (!tmp.empty()) AE_CHECK(cudaStreamSynchronize(op->st));
+    });
+}
+
+int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fab* dw, ae_fab* w) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(dw || w, "NewtonDW: nothing to compute");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        require(op->amr[amrlev].model_set, "SetModel has not been called on this level", AE_ERR_STATE);
+        const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "NewtonDW u");
+        if (F0) check_fab(F0, v, 9, "NewtonDW F0");
+        if (dw) check_fab(dw, v, 9, "NewtonDW dw");
+        if (w) check_fab(w, v, 1, "NewtonDW w");
+        require(op->model != AE_MODEL_DIAGONAL || !F0, "NewtonDW: no affine form of the diagonal model");
+        require(is_device_ptr(u->data) && (!F0 || is_device_ptr(F0->data)) && (!dw || is_device_ptr(dw->data)) &&
+                    (!w || is_device_ptr(w->data)),
+                "NewtonDW: fabs must be device memory");
+        const double half = (op->model == AE_MODEL_ISOTROPIC && F0) ? 1.0 : 0.5;
+        launch_newton_post(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
+                           F0 ? cview(fab_view<double>(*F0)) : View<const double>{},
+                           dw ? fab_view<double>(*dw) : View<double>{}, w ? fab_view<double>(*w) : View<double>{}, half,
+                           op->st);
     });
 }
 

@@ -174,6 +174,148 @@ void launch_energy(const OpParams& P, View<const double> C, View<const double> u
     launched();
 }
 
+// ------------------------------------------------------------------ Solver::Nonlocal::Newton<T>
+// DW(grad u) = C : (grad u - F0) for the linear and affine models (kinematic variable grad u:
+// src/Model/Solid/Linear/Cubic.H:64-67, src/Model/Solid/Affine/Cubic.H:38-41).
+// grad u with Numeric::GetStencil relative to the box bx (one-sided on its faces).
+__device__ __forceinline__ void grad_box(const Box3& bx, const SCoef<double>& K, const View<const double>& u, int i,
+                                         int j, int k, double gu[3][3]) {
+    const int ci[3] = {i, j, k};
+    const long long os[3] = {1, u.sy, u.sz};
+    const long long o = u.at(i, j, k);
+    for (int p = 0; p < 3; ++p) {
+        const double* up = u.p + o + p * u.sc;
+        for (int d = 0; d < 3; ++d) {
+            const long long s = os[d];
+            if (ci[d] == bx.lo[d]) gu[p][d] = (up[s] - up[0]) * K.id[d];
+            else if (ci[d] == bx.hi[d]) gu[p][d] = (up[0] - up[-s]) * K.id[d];
+            else gu[p][d] = (up[s] - up[-s]) * K.h[d];
+        }
+    }
+}
+template <int M>
+__device__ __forceinline__ void newton_sigma(const View<const double>& C, const View<const double>& F0, int i, int j,
+                                             int k, double gu[3][3], double s[3][3]) {
+    constexpr int NC = NCoef<M>::value;
+    double a[NC];
+    const long long cc = C.at(i, j, k);
+    for (int q = 0; q < NC; ++q) a[q] = C.p[cc + q * C.sc];
+    if (F0.p) {
+        const long long of = F0.at(i, j, k);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) gu[p][d] -= F0.p[of + (3 * p + d) * F0.sc];
+    }
+    stress_of<M, double>(a, gu, s);
+}
+// dw on bx2 = grow(valid, 2) ∩ domain (src/Solver/Nonlocal/Newton.H:45-76)
+template <int M>
+__global__ void __launch_bounds__(kBlock) k_newton_dw(SCoef<double> K, Reg reg, Box3 bx2, View<const double> C,
+                                                      View<const double> u, View<const double> F0, View<double> dw) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3], s[3][3];
+    grad_box(bx2, K, u, i, j, k, gu);
+    newton_sigma<M>(C, F0, i, j, k, gu, s);
+    const long long o = dw.at(i, j, k);
+    for (int p = 0; p < 3; ++p)
+        for (int d = 0; d < 3; ++d) dw.p[o + (3 * p + d) * dw.sc] = s[p][d];
+}
+// rhs on bx1 = grow(valid, 1) ∩ domain (src/Solver/Nonlocal/Newton.H:80-135): BC rows with
+// sigma = dw on the domain boundary (faces classified against bx1), b - div(dw) inside
+__global__ void __launch_bounds__(kBlock) k_newton_rhs(Geo g, BCP bc, SCoef<double> K, Reg reg, Box3 bx1,
+                                                       View<const double> u, View<const double> b,
+                                                       View<const double> dw, View<double> rhs) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long ob = b.at(i, j, k), orr = rhs.at(i, j, k), ow = dw.at(i, j, k);
+    const bool bnd = i == g.dlo[0] || i == g.dhi[0] || j == g.dlo[1] || j == g.dhi[1] || k == g.dlo[2] ||
+                     k == g.dhi[2];
+    if (bnd) {
+        double gu[3][3], s[3][3], n[3];
+        grad_box(bx1, K, u, i, j, k, gu);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) s[p][d] = dw.p[ow + (3 * p + d) * dw.sc];
+        Geo gb = g;
+        for (int d = 0; d < 3; ++d) { gb.dlo[d] = bx1.lo[d]; gb.dhi[d] = bx1.hi[d]; }
+        const int face = classify<double>(gb, i, j, k, n);
+        const long long ou = u.at(i, j, k);
+        for (int r = 0; r < 3; ++r) {
+            double v = 0.0;
+            if (face >= 0) {
+                const unsigned char tp = bc.t[face][r];
+                if (tp == DISP) v = u.p[ou + r * u.sc];
+                else if (tp == TRAC) v = s[r][0] * n[0] + s[r][1] * n[1] + s[r][2] * n[2];
+                else if (tp == NEUMANN) v = gu[r][0] * n[0] + gu[r][1] * n[1] + gu[r][2] * n[2];
+            }
+            rhs.p[orr + r * rhs.sc] = b.p[ob + r * b.sc] - v;
+        }
+        return;
+    }
+    const long long os[3] = {1, dw.sy, dw.sz};
+    for (int p = 0; p < 3; ++p) {
+        double div = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double* w = dw.p + ow + (3 * p + d) * dw.sc;
+            div += (w[os[d]] - w[-os[d]]) / 2. / g.dx[d];
+        }
+        rhs.p[orr + p * rhs.sc] = b.p[ob + p * b.sc] - div;
+    }
+}
+// Newton::DW and Newton::W on valid ∩ domain, stencils relative to the domain
+// (src/Solver/Nonlocal/Newton.H:233-333); half = 0.5, or 1 for Affine::Isotropic
+// (src/Model/Solid/Affine/Isotropic.H:31-34)
+template <int M>
+__global__ void __launch_bounds__(kBlock) k_newton_post(Geo g, SCoef<double> K, Reg reg, View<const double> C,
+                                                        View<const double> u, View<const double> F0, View<double> dw,
+                                                        View<double> w, double half) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3], s[3][3];
+    grad_at(g, K, u, i, j, k, gu);
+    newton_sigma<M>(C, F0, i, j, k, gu, s);  // gu now holds grad u - F0
+    if (dw.p) {
+        const long long o = dw.at(i, j, k);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) dw.p[o + (3 * p + d) * dw.sc] = s[p][d];
+    }
+    if (w.p) {
+        double tr = 0.0;
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) tr += gu[p][d] * s[p][d];
+        w.p[w.at(i, j, k)] = half * tr;
+    }
+}
+void launch_newton_residual(const OpParams& P, View<const double> C, View<const double> u, View<const double> b,
+                            View<const double> F0, View<double> dw, View<double> rhs, cudaStream_t st) {
+    const Box3 bx2 = box_isect(box_isect(box_grow(geo_valid(P.g), 2), geo_domain(P.g)), geo_store(P.g));
+    const Box3 bx1 = box_isect(box_isect(box_grow(geo_valid(P.g), 1), geo_domain(P.g)), geo_store(P.g));
+    const SCoef<double> K = make_scoef<double>(P.g);
+    const Reg r2 = make_reg(bx2), r1 = make_reg(bx1);
+    if (r2.n == 0) return;
+    dispatch_model<double>(P.model, [&](auto m) {
+        k_newton_dw<decltype(m)::value><<<nblocks(r2.n), kBlock, 0, st>>>(K, r2, bx2, C, u, F0, dw);
+    });
+    launched();
+    k_newton_rhs<<<nblocks(r1.n), kBlock, 0, st>>>(P.g, P.bc, K, r1, bx1, u, b, cview(dw), rhs);
+    launched();
+}
+void launch_newton_post(const OpParams& P, View<const double> C, View<const double> u, View<const double> F0,
+                        View<double> dw, View<double> w, double half, cudaStream_t st) {
+    const Reg reg = make_reg(box_isect(geo_valid(P.g), geo_domain(P.g)));
+    if (reg.n == 0) return;
+    dispatch_model<double>(P.model, [&](auto m) {
+        k_newton_post<decltype(m)::value><<<nblocks(reg.n), kBlock, 0, st>>>(P.g, make_scoef<double>(P.g), reg, C, u,
+                                                                              F0, dw, w, half);
+    });
+    launched();
+}
+
 // ------------------------------------------------------------------ bottom solve (one CTA)
 // MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab (krylov_bottom); the whole
 // Krylov loop runs inside one thread block on the coarsest level (ng = 0, storage = domain).

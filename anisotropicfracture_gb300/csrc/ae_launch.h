@@ -152,6 +152,12 @@ void launch_stress(const OpParams& P, View<const double> C, View<const double> u
                    cudaStream_t st);
 void launch_energy(const OpParams& P, View<const double> C, View<const double> u, View<double> w, cudaStream_t st);
 
+// Newton<T>: rhs = b - N(u) (dw: 9-component scratch over the level's storage; F0.p may be null)
+void launch_newton_residual(const OpParams& P, View<const double> C, View<const double> u, View<const double> b,
+                            View<const double> F0, View<double> dw, View<double> rhs, cudaStream_t st);
+// Newton::DW (dw.p may be null) and Newton::W (w.p may be null) on valid ∩ domain
+void launch_newton_post(const OpParams& P, View<const double> C, View<const double> u, View<const double> F0,
+                        View<double> dw, View<double> w, double half, cudaStream_t st);
 // Voronoi stiffness over `region`: ids (int32 per node) -> gid (uint16) and the per-node FP64
 // stiffness C = tab[id]; tab32 = (float) tab.  *bad is set if an id is outside [0, ng).
 void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned short> gid, View<double> C,

@@ -241,6 +241,22 @@ class Elastic:
         fs, fu = sigma.fab(), u.fab()
         check(load().ae_stress(self._h, amrlev, C.byref(fs), C.byref(fu), int(bool(voigt))))
 
+    def NewtonResidual(self, amrlev, rhs, u, b, F0=None):
+        """rhs = b - N(u) (Newton<T>::prepareForSolve); device Fields."""
+        fr, fu, fb = rhs.fab(), u.fab(), b.fab()
+        f0 = F0.fab() if F0 is not None else None
+        check(load().ae_newton_residual(self._h, amrlev, C.byref(fu), C.byref(fb),
+                                        C.byref(f0) if f0 is not None else None, C.byref(fr)))
+
+    def NewtonDW(self, amrlev, u, dw=None, w=None, F0=None):
+        """Newton<T>::DW (9 components) and Newton<T>::W; device Fields."""
+        fu = u.fab()
+        fd = dw.fab() if dw is not None else None
+        fw = w.fab() if w is not None else None
+        f0 = F0.fab() if F0 is not None else None
+        check(load().ae_newton_dw(self._h, amrlev, C.byref(fu), C.byref(f0) if f0 is not None else None,
+                                  C.byref(fd) if fd is not None else None, C.byref(fw) if fw is not None else None))
+
     def Energy(self, amrlev, energy, u, homogeneous=False):
         fw, fu = energy.fab(), u.fab()
         check(load().ae_energy(self._h, amrlev, C.byref(fw), C.byref(fu)))
@@ -322,9 +338,10 @@ class Linear:
 
 
 class Newton(Linear):
-    """Solver::Nonlocal::Newton<T> for the linear models: with a zero initial displacement and
-    one Newton iteration (the reference default, Newton.H:337) the solve reduces to one
-    Linear::solve of A u = b."""
+    """Solver::Nonlocal::Newton<T> (src/Solver/Nonlocal/Newton.H:141-205) for the linear and
+    affine models: m_nriters times, rhs = b - N(u) (ae_newton_residual), one Linear::solve of the
+    correction (its previous value is the initial guess, as the reference keeps dsol), u += dsol.
+    F0: per-level eigenstrain Fields (9 components) of an Affine model, or None."""
 
     def __init__(self, op):
         super().__init__(op)
@@ -333,5 +350,32 @@ class Newton(Linear):
     def setNRIters(self, n):
         self.m_nriters = int(n)
 
-    def solve(self, u, b, model=None, tol_rel=None, tol_abs=None):
-        return Linear.solve(self, u, b, tol_rel, tol_abs)
+    def solve(self, u, b, model=None, tol_rel=None, tol_abs=None, F0=None):
+        import torch
+        u = u if isinstance(u, (list, tuple)) else [u]
+        b = b if isinstance(b, (list, tuple)) else [b]
+        F0 = [None] * len(u) if F0 is None else (F0 if isinstance(F0, (list, tuple)) else [F0])
+
+        def dev(f):  # device copy of a host Field, or the Field itself
+            if f is None or not isinstance(f.arr, np.ndarray):
+                return f
+            return Field(torch.from_numpy(np.ascontiguousarray(f.arr)).cuda(), f.lo)
+
+        ud, bd, fd = [dev(f) for f in u], [dev(f) for f in b], [dev(f) for f in F0]
+        dsol = [Field(torch.zeros_like(f.arr), f.lo) for f in ud]
+        rhs = [Field(f.arr.clone(), f.lo) for f in bd]
+        res = None
+        for _ in range(self.m_nriters):
+            for lev in range(len(ud)):
+                fu, fb, fr = ud[lev].fab(), bd[lev].fab(), rhs[lev].fab()
+                f0 = fd[lev].fab() if fd[lev] is not None else None
+                check(load().ae_newton_residual(self.linop.handle, lev, C.byref(fu), C.byref(fb),
+                                                C.byref(f0) if f0 is not None else None, C.byref(fr)))
+            res = Linear.solve(self, dsol, rhs, tol_rel, tol_abs)
+            for lev in range(len(ud)):
+                ud[lev].arr += dsol[lev].arr
+        torch.cuda.synchronize()
+        for f, g in zip(u, ud):
+            if isinstance(f.arr, np.ndarray):
+                f.arr[...] = g.arr.cpu().numpy()
+        return res

@@ -166,6 +166,20 @@ int ae_bc_init(ae_op* op, int amrlev, const ae_fab* rhs, int homogeneous);
 int ae_strain(ae_op* op, int amrlev, const ae_fab* eps, const ae_fab* u, int voigt);
 int ae_stress(ae_op* op, int amrlev, const ae_fab* sig, const ae_fab* u, int voigt);
 int ae_energy(ae_op* op, int amrlev, const ae_fab* w, const ae_fab* u);
+/* Solver::Nonlocal::Newton<T>::prepareForSolve (src/Solver/Nonlocal/Newton.H:30-139) for the
+ * linear and affine models (DW = C : (grad u - F0), src/Model/Solid/Affine/Cubic.H:38-41):
+ * rhs = b - N(u) on grow(valid, 1) ∩ domain, N(u) = BC rows with sigma = DW on the domain
+ * boundary (faces classified against that box) and the central divergence of DW inside, DW from
+ * one-sided gradients at the faces of grow(valid, 2) ∩ domain.  F0: 9 components (row-major
+ * eigenstrain, an Affine model) or NULL.  u and F0 cover grow(valid, 2) ∩ domain, b and rhs
+ * grow(valid, 1) ∩ domain; FP64, host or device memory (host fabs are staged and the call then
+ * synchronises).  Other nodes of rhs are not written. */
+int ae_newton_residual(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, const ae_fab* F0, ae_fab* rhs);
+/* Newton<T>::DW (9 components, row-major) and Newton<T>::W on valid ∩ domain
+ * (src/Solver/Nonlocal/Newton.H:233-333); either output may be NULL.  W = 1/2 G : C G,
+ * G = grad u - F0, except Affine::Isotropic (isotropic model with F0) whose W has no 1/2
+ * (src/Model/Solid/Affine/Isotropic.H:31-34). */
+int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fab* dw, ae_fab* w);
 
 /* Solver::Nonlocal::Linear::solve (Linear.H:102-112) -> MLMG::solve.
  * sol and rhs: one fab per AMR level, host or device; sol holds the initial guess.

@@ -292,18 +292,45 @@ protected:
     double m_tol_rel = 1e-8, m_tol_abs = 1e-8;
 };
 
-// Newton<T> for the linear models: u0 = 0 and one NR iteration reduce to one Linear::solve
-// (Newton.H:142-209).
+// Newton<T>::solve (src/Solver/Nonlocal/Newton.H:141-205) for the linear and affine models:
+// m_nriters times, rhs = b - N(u) (ae_newton_residual), one Linear::solve of the correction
+// (starting from the previous correction, as the reference keeps dsol), u += dsol.  F0: one
+// 9-component eigenstrain fab per level for an Affine model, or none.
 template <class T>
 class Newton : public Linear {
 public:
-    explicit Newton(Operator::Elastic<T>& op) : Linear(op) {}
+    explicit Newton(Operator::Elastic<T>& op) : Linear(op), m_op(op) {}
     void setNRIters(int n) { m_nriters = n; }
-    double solve(std::vector<alamo::Fab>& u, std::vector<alamo::Fab>& b, double tol_rel, double tol_abs) {
-        return Linear::solve(u, b, tol_rel, tol_abs);
+    double solve(std::vector<alamo::Fab>& u, std::vector<alamo::Fab>& b, double tol_rel, double tol_abs,
+                 const std::vector<alamo::Fab>* F0 = nullptr) {
+        const size_t nl = u.size();
+        std::vector<std::vector<double>> dbuf(nl), rbuf(nl);
+        std::vector<alamo::Fab> dsol(nl), rhs(nl);
+        for (size_t l = 0; l < nl; ++l) {
+            const size_t n = (size_t)b[l].npts() * b[l].ncomp;
+            dbuf[l].assign((size_t)u[l].npts() * u[l].ncomp, 0.0);
+            rbuf[l].assign(b[l].data, b[l].data + n);
+            dsol[l] = alamo::Fab(dbuf[l].data(), u[l].lo, u[l].hi, u[l].ncomp);
+            rhs[l] = alamo::Fab(rbuf[l].data(), b[l].lo, b[l].hi, b[l].ncomp);
+        }
+        double res = 0.0;
+        for (int it = 0; it < m_nriters; ++it) {
+            for (size_t l = 0; l < nl; ++l) {
+                const ae_fab fu = u[l].c(), fb = b[l].c();
+                ae_fab fr = rhs[l].c();
+                ae_fab f0{};
+                if (F0) f0 = (*F0)[l].c();
+                alamo::check(ae_newton_residual(m_op.handle(), (int)l, &fu, &fb, F0 ? &f0 : nullptr, &fr));
+            }
+            res = Linear::solve(dsol, rhs, tol_rel, tol_abs);
+            for (size_t l = 0; l < nl; ++l)
+                for (size_t q = 0; q < dbuf[l].size(); ++q) u[l].data[q] += dbuf[l][q];
+        }
+        return res;
     }
 
 private:
+    Operator::Elastic<T>& m_op;
     int m_nriters = 1;
 };
 }  // namespace Nonlocal

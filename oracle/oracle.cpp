@@ -1600,3 +1600,118 @@ int orc_rve_solve(const orc_rve_level* L0, int model, const double* C, const dou
 }
 
 }  // extern "C"
+
+// ================================================================ Solver::Nonlocal::Newton<T>
+// For the linear and affine models the kinematic variable is grad u and DW(grad u) =
+// C : (grad u - F0) (src/Model/Solid/Linear/Cubic.H:64-67, src/Model/Solid/Affine/Cubic.H:38-41,
+// src/Model/Solid/Affine/Isotropic.H:35-38); F0 = 0 for the Linear models.
+namespace {
+
+// GetStencil relative to an arbitrary box (src/Numeric/Stencil.H:12-34)
+inline void box_stencil(const Box& b, int i, int j, int k, int st[3]) {
+    const int c[3] = {i, j, k};
+    for (int d = 0; d < 3; ++d) st[d] = (c[d] == b.lo[d]) ? ST_HI : (c[d] == b.hi[d]) ? ST_LO : ST_CEN;
+}
+
+inline void newton_grad(const Lev& L, const double* U, const int st[3], long c, double g[3][3]) {
+    for (int p = 0; p < 3; ++p)
+        for (int d = 0; d < 3; ++d) g[p][d] = D1(U + p * L.nn + c, L.stride(d), L.dx[d], st[d]);
+}
+
+// sig = DW(grad u) at node c
+inline void newton_dw_node(const Lev& L, int model, const double* C, const double* F0, const double g[3][3], long c,
+                           double sig[3][3]) {
+    const int nc = ncoef_of(model);
+    double a[21], e[3][3];
+    for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
+    for (int p = 0; p < 3; ++p)
+        for (int d = 0; d < 3; ++d) e[p][d] = g[p][d] - (F0 ? F0[(3 * p + d) * L.nn + c] : 0.0);
+    stress_of(model, a, e, sig);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Newton::prepareForSolve (src/Solver/Nonlocal/Newton.H:30-139) on one box: dw = DW(grad u) on
+// grow(valid, 2) ∩ domain, stencils one-sided at that box's faces; then on grow(valid, 1) ∩ domain
+// rhs = b - BC(u, grad u, dw) on the domain boundary (BC faces classified against that box) and
+// rhs = b - div(dw) by central differences inside.  Nodes outside keep rhs.
+int orc_newton_residual(const orc_level* L0, int model, const double* C, const int* bctype, const double* u,
+                        const double* b, const double* F0, double* rhs) {
+    const Lev L(*L0);
+    const Box bx2 = isect(isect(grow(L.valid, 2), L.dom), L.store);
+    std::vector<double> dw(9 * L.nn, 0.0);
+    for_box(bx2, [&](int i, int j, int k) {
+        int st[3];
+        box_stencil(bx2, i, j, k, st);
+        const long c = L.at(i, j, k);
+        double g[3][3], s[3][3];
+        newton_grad(L, u, st, c, g);
+        newton_dw_node(L, model, C, F0, g, c, s);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) dw[(3 * p + d) * L.nn + c] = s[p][d];
+    });
+    const Box bx1 = isect(isect(grow(L.valid, 1), L.dom), L.store);
+    for_box(bx1, [&](int i, int j, int k) {
+        const long c = L.at(i, j, k);
+        const int m[3] = {i, j, k};
+        bool bnd = false;
+        for (int d = 0; d < 3; ++d) bnd = bnd || m[d] == L.dom.lo[d] || m[d] == L.dom.hi[d];
+        if (bnd) {
+            int st[3];
+            box_stencil(bx1, i, j, k, st);
+            double g[3][3], s[3][3], uu[3], nrm[3], f[3] = {0, 0, 0};
+            newton_grad(L, u, st, c, g);
+            for (int p = 0; p < 3; ++p) {
+                uu[p] = u[p * L.nn + c];
+                for (int d = 0; d < 3; ++d) s[p][d] = dw[(3 * p + d) * L.nn + c];
+            }
+            const int face = classify(bx1, i, j, k, nrm);
+            if (face >= 0) bc_set(bctype + 3 * face, uu, g, s, nrm, f);
+            for (int p = 0; p < 3; ++p) rhs[p * L.nn + c] = b[p * L.nn + c] - f[p];
+        } else {
+            for (int p = 0; p < 3; ++p) {
+                const double* w0 = &dw[(3 * p + 0) * L.nn + c];
+                const double* w1 = &dw[(3 * p + 1) * L.nn + c];
+                const double* w2 = &dw[(3 * p + 2) * L.nn + c];
+                rhs[p * L.nn + c] = b[p * L.nn + c] - ((w0[L.sx] - w0[-L.sx]) / 2. / L.dx[0] +
+                                                       (w1[L.sy] - w1[-L.sy]) / 2. / L.dx[1] +
+                                                       (w2[L.sz] - w2[-L.sz]) / 2. / L.dx[2]);
+            }
+        }
+    });
+    return 0;
+}
+
+// Newton::DW / Newton::W (src/Solver/Nonlocal/Newton.H:233-333) on the valid box, stencils
+// relative to the domain.  dw: 9 components, row-major (dw(0) = sig(0,0), dw(1) = sig(0,1), ...).
+// W(grad u) = 0.5 tr((G)^T C G), G = grad u - F0 (src/Model/Solid/Linear/Cubic.H:60-63,
+// Affine/Cubic.H:34-37); Affine::Isotropic has no factor 0.5 (src/Model/Solid/Affine/Isotropic.H:31-34),
+// applied when model is isotropic and F0 is given.
+int orc_newton_dw(const orc_level* L0, int model, const double* C, const double* u, const double* F0, double* dw,
+                  double* w) {
+    const Lev L(*L0);
+    const Box v = isect(L.valid, L.dom);
+    const double half = (model == ORC_ISOTROPIC && F0) ? 1.0 : 0.5;
+    for_box(v, [&](int i, int j, int k) {
+        int st[3];
+        get_stencil(L, i, j, k, st);
+        const long c = L.at(i, j, k);
+        double g[3][3], s[3][3];
+        newton_grad(L, u, st, c, g);
+        newton_dw_node(L, model, C, F0, g, c, s);
+        if (dw)
+            for (int p = 0; p < 3; ++p)
+                for (int d = 0; d < 3; ++d) dw[(3 * p + d) * L.nn + c] = s[p][d];
+        if (w) {
+            double tr = 0.0;
+            for (int p = 0; p < 3; ++p)
+                for (int d = 0; d < 3; ++d) tr += (g[p][d] - (F0 ? F0[(3 * p + d) * L.nn + c] : 0.0)) * s[p][d];
+            w[c] = half * tr;
+        }
+    });
+    return 0;
+}
+
+}  // extern "C"

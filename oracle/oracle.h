@@ -97,6 +97,14 @@ int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const*
 /* number of multigrid levels the solver builds for this level */
 int orc_num_mg_levels(const orc_level* L, int max_mg_levels);
 
+/* Solver::Nonlocal::Newton<T> pieces for the linear / affine models: the Newton right-hand side
+ * rhs = b - N(u) (DW = C : (grad u - F0); F0: 9 components row-major, or NULL) and the DW / W
+ * post-processing fields (dw: 9 components, w: 1; either may be NULL). */
+int orc_newton_residual(const orc_level* L, int model, const double* C, const int* bctype, const double* u,
+                        const double* b, const double* F0, double* rhs);
+int orc_newton_dw(const orc_level* L, int model, const double* C, const double* u, const double* F0, double* dw,
+                  double* w);
+
 /* ---- periodic cells (homogenisation): n[0] n[1] n[2] unique nodes, no ghosts ----
  * w periodic, u = E x + w; A w + c = b with b = -sum_d (d_d C) : E e_d, mean(w) = 0 and c a
  * uniform body force (the multiplier of the mean constraint; see oracle.cpp). */

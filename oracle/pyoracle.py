@@ -265,6 +265,35 @@ def node_coords(L):
     return X, Y, Z
 
 
+# ---------------------------------------------------------------- Newton pieces
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def newton_residual(L, model, Cf, bctype, u, b, F0=None, rhs=None):
+    """rhs = b - N(u) on grow(valid, 1) ∩ domain (other nodes keep rhs, default b)."""
+    lb = lib()
+    d = C.POINTER(C.c_double)
+    lb.orc_newton_residual.argtypes = [C.POINTER(Level), C.c_int, d, C.POINTER(C.c_int), d, d, d, d]
+    out = np.array(b, dtype=np.float64, copy=True) if rhs is None else np.array(rhs, dtype=np.float64, copy=True)
+    Cf, u, b, F0 = _f64(Cf), _f64(u), _f64(b), _f64(F0)  # kept alive across the call
+    bt, bp = _i(bctype)
+    lb.orc_newton_residual(C.byref(L), model, _d(Cf), bp, _d(u), _d(b), None if F0 is None else _d(F0), _d(out))
+    return out
+
+
+def newton_dw(L, model, Cf, u, F0=None):
+    """(dw: 9 x shape, w: shape) on the valid box."""
+    lb = lib()
+    d = C.POINTER(C.c_double)
+    lb.orc_newton_dw.argtypes = [C.POINTER(Level), C.c_int, d, d, d, d, d]
+    dw = np.zeros((9,) + L.shape)
+    w = np.zeros(L.shape)
+    Cf, u, F0 = _f64(Cf), _f64(u), _f64(F0)
+    lb.orc_newton_dw(C.byref(L), model, _d(Cf), _d(u), None if F0 is None else _d(F0), _d(dw), _d(w))
+    return dw, w
+
+
 # ---------------------------------------------------------------- periodic cells
 class RveLevel(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("pad_", C.c_int), ("dx", C.c_double * 3)]
