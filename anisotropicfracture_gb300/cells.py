@@ -221,6 +221,21 @@ class CellServer:
             pass
 
 
+# ---------------------------------------------------------------- multi-GPU sharding
+def partition_cells(cell_bytes, nranks):
+    """Assign cells to ranks: largest first, each to the rank with the fewest bytes so far (ties
+    to the lower rank).  Deterministic, so every rank computes the same assignment without a
+    collective.  Returns one list of cell indices per rank, each in increasing order."""
+    order = sorted(range(len(cell_bytes)), key=lambda c: (-cell_bytes[c], c))
+    load = [0] * nranks
+    parts = [[] for _ in range(nranks)]
+    for c in order:
+        r = min(range(nranks), key=lambda q: (load[q], q))
+        parts[r].append(c)
+        load[r] += cell_bytes[c]
+    return [sorted(p) for p in parts]
+
+
 # ---------------------------------------------------------------- synthetic cells
 def rve_grains(n, ngrains, seed, length=1.0, C11=1.68, C12=1.21, C44=0.75):
     """Seeds (ngrains x 3, uniform in the cell) and cubic tables (Haar-uniform rotations) of a

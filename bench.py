@@ -342,30 +342,58 @@ def cpu_cells_sample(work, nsample, threads=None):
     return secs, nodes
 
 
-def bench_batch(args, lib):
-    """Batched cells: mixed and FP64 in one batch, FP64 one cell at a time, CPU oracle sample."""
-    work = batch_workload(args.batch_cells)
-    nodes = sum(w["n"] ** 3 for w in work)
+def _max_over_ranks(x, world):
+    """Max of a host float over the ranks (the slowest rank bounds a weak-scaling step)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def bench_batch(args, lib, rank=0, world=1):
+    """Batched cells: mixed and FP64 in one batch, FP64 one cell at a time, CPU oracle sample.
+    With N ranks each takes its largest-first share of the cells (no collective on the data path)
+    and times are the max over ranks; solves/s count all ranks' cells (weak scaling)."""
+    from anisotropicfracture_gb300 import cells as _cells
+    work_all = batch_workload(args.batch_cells)
+    if world > 1:
+        share = _cells.partition_cells([_cells.plan_bytes(w["n"]) for w in work_all], world)[rank]
+        work = [work_all[c] for c in share]
+    else:
+        work = work_all
+    total = len(work_all)
+    nodes = sum(w["n"] ** 3 for w in work_all)
     t0 = time.perf_counter()
     B = make_cell_batch(work)
     setup_s = time.perf_counter() - t0
     out = {"workload": "%d periodic polycrystal RVEs, edges uniform in %s cells (seed 4), 8-32 grains each, "
-                       "cubic 1.68/1.21/0.75, exx = 1e-3, tol_rel 1e-8" % (len(work), list(BATCH_EDGES)),
-           "cells": len(work), "nodes": nodes, "device_bytes": B.device_bytes(), "setup_s": setup_s,
+                       "cubic 1.68/1.21/0.75, exx = 1e-3, tol_rel 1e-8" % (total, list(BATCH_EDGES)),
+           "cells": total, "nodes": nodes, "device_bytes": B.device_bytes(), "setup_s": setup_s,
            "cycle": "V-cycle, 2 pre + 2 post smoother calls of 2 damped-Jacobi sweeps, BiCGStab bottom",
-           "inner_cycles": args.batch_inner, "unit": UNIT}
+           "inner_cycles": args.batch_inner, "unit": UNIT,
+           "ranks": world, "scaling": "weak" if world > 1 else None}
     res = {}
     sols = {}
     for prec, name in ((1, "mixed"), (0, "fp64_batched")):
         st, rc = B.solve(precision=prec, inner_cycles=args.batch_inner, check=False, **CELL_SOLVER)  # warm/tune
         l0 = lib.ae_kernel_launches()
+        _barrier(world)
         t0 = time.perf_counter()
         reps = max(1, args.batch_steps)
         for _ in range(reps):
             st, rc = B.solve(precision=prec, inner_cycles=args.batch_inner, check=False, **CELL_SOLVER)
-        secs = (time.perf_counter() - t0) / reps
+        secs = _max_over_ranks((time.perf_counter() - t0) / reps, world)
         launches = (lib.ae_kernel_launches() - l0) // reps
-        res[name] = {"value": len(work) / secs, "s_per_batch": secs, "converged": rc == 0,
+        res[name] = {"value": total / secs, "s_per_batch": secs, "converged": rc == 0,
                      "max_iters": max(s["iters"] for s in st), "mean_iters": float(np.mean([s["iters"] for s in st])),
                      "gpu_launches": int(launches)}
         sols[name] = [B.solution(s) for s in range(len(work))]
@@ -376,16 +404,18 @@ def bench_batch(args, lib):
     singles = [make_cell_batch([w]) for w in work[:lim]]
     for Bs in singles[:2]:
         Bs.solve(precision=0, check=False, **CELL_SOLVER)
+    _barrier(world)
     t0 = time.perf_counter()
     ok = True
     for Bs in singles:
         st, rc = Bs.solve(precision=0, check=False, **CELL_SOLVER)
         ok = ok and rc == 0
-    secs = time.perf_counter() - t0
+    secs = _max_over_ranks(time.perf_counter() - t0, world)
     w64 = [Bs.solution(0) for Bs in singles]
     for Bs in singles:
         Bs.close()
-    res["fp64_one_at_a_time"] = {"value": lim / secs, "cells_timed": lim, "seconds": secs, "converged": ok}
+    timed = lim * world if args.batch_single_limit > 0 else total
+    res["fp64_one_at_a_time"] = {"value": timed / secs, "cells_timed": timed, "seconds": secs, "converged": ok}
     err = 0.0
     for a, b in zip(sols["mixed"][:lim], w64):
         err = max(err, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
@@ -397,12 +427,12 @@ def bench_batch(args, lib):
     out["displacement_err_mixed_vs_fp64"] = err
     out["fp64_batched_vs_one_at_a_time"] = err_b
     out["shapes"] = shapes
-    if not args.no_cpu:
+    if not args.no_cpu and rank == 0:
         try:
             ns = max(1, args.batch_cpu_sample)
             secs, nn = cpu_cells_sample(work, ns, threads=os.cpu_count())
             per_node = secs / nn
-            out["cpu_baseline"] = {"value": 1.0 / (per_node * nodes / len(work)), "unit": UNIT,
+            out["cpu_baseline"] = {"value": 1.0 / (per_node * nodes / total), "unit": UNIT,
                                    "cores": os.cpu_count(), "kind": "port",
                                    "sample": "FP64 oracle cell solves of the first %d cells (%d nodes, %.1f s), "
                                              "scaled per node to the mean cell" % (ns, nn, secs)}
@@ -690,7 +720,13 @@ def main():
 
 
 def add_cell_workloads(args, lib, line, rank, world):
-    """The damaged-polycrystal, batched and served cell workloads (rank 0 of a single-GPU run)."""
+    """The damaged-polycrystal, batched and served cell workloads.  The batch shards over ranks;
+    the single-box damaged solve and the server (one request loop per GPU) run on a 1-GPU job."""
+    if not args.no_batch:
+        try:
+            line["batch"] = bench_batch(args, lib, rank, world)
+        except Exception as e:  # pragma: no cover
+            line["batch"] = {"error": str(e)}
     if world > 1 or rank != 0:
         return
     if not args.no_config2:
@@ -698,11 +734,6 @@ def add_cell_workloads(args, lib, line, rank, world):
             line["config2"] = bench_config2(args)
         except Exception as e:  # pragma: no cover
             line["config2"] = {"error": str(e)}
-    if not args.no_batch:
-        try:
-            line["batch"] = bench_batch(args, lib)
-        except Exception as e:  # pragma: no cover
-            line["batch"] = {"error": str(e)}
     if not args.no_serve:
         try:
             line["serve"] = bench_serve(args)
