@@ -31,24 +31,29 @@ def _dev(a):
 @pytest.mark.parametrize("affine", [False, True])
 def test_newton_residual_matches_oracle(model, fine, affine):
     rng = np.random.default_rng(10 + model + 2 * fine + 4 * affine)
-    L = po.amr_levels(8, 2)[1] if fine else po.level((9, 8, 7))
-    Cf = random_coeffs(model, L.shape, rng)
+    # a refined patch with ghost nodes (AMR level 1 of a two-level operator), or a single level
+    Ls = po.amr_levels(8, 2) if fine else [po.level((9, 8, 7))]
+    a = len(Ls) - 1
+    L = Ls[a]
+    Cs = [random_coeffs(model, Lk.shape, rng) for Lk in Ls]
+    Cf = Cs[a]
     bc = bc_random(rng)
     u = rng.standard_normal((3,) + L.shape)
     b = rng.standard_normal((3,) + L.shape)
     F0 = 0.1 * rng.standard_normal((9,) + L.shape) if affine else None
     ref = po.newton_residual(L, model, Cf, bc.type, u, b, F0=F0)
-    op = Elastic([_desc(L)], model)
-    op.SetModel(0, Field(Cf, _lo(L)))
+    op = Elastic([_desc(Lk) for Lk in Ls], model)
+    for k, Lk in enumerate(Ls):
+        op.SetModel(k, Field(Cs[k], _lo(Lk)))
     op.SetBC(bc)
     rd = _dev(b.copy())
-    op.NewtonResidual(0, Field(rd, _lo(L)), Field(_dev(u), _lo(L)), Field(_dev(b), _lo(L)),
+    op.NewtonResidual(a, Field(rd, _lo(L)), Field(_dev(u), _lo(L)), Field(_dev(b), _lo(L)),
                       Field(_dev(F0), _lo(L)) if affine else None)
     torch.cuda.synchronize()
     assert normwise_err(rd.cpu().numpy(), ref) < TOL
     # host fabs take the staged path and give the same values
     rh = b.copy()
-    op.NewtonResidual(0, Field(rh, _lo(L)), Field(u, _lo(L)), Field(b, _lo(L)),
+    op.NewtonResidual(a, Field(rh, _lo(L)), Field(u, _lo(L)), Field(b, _lo(L)),
                       Field(np.ascontiguousarray(F0), _lo(L)) if affine else None)
     assert np.array_equal(rh, rd.cpu().numpy())
     op.close()
