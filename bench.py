@@ -49,6 +49,10 @@ FAPPLY32_BYTES_PER_NODE = 108
 JACOBI32_BYTES_PER_NODE_GRAINS = 12 + 12 + 12 + 2 + 12
 FAPPLY64_BYTES_PER_NODE_GRAINS = 24 + 2 + 24
 FAPPLY32_BYTES_PER_NODE_GRAINS = 12 + 2 + 12
+# measured DRAM bytes per node of the FP32 Jacobi sweep (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum at 193^3, larger than L2; profiles/jacobi32_dram_193cubed.md), keyed by
+# grain map on/off; 0 = not measured
+JACOBI32_TRAFFIC_PER_NODE = {True: 0, False: 0}
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
 # time to a full solve in the reference arm, which cannot afford a full CPU solve.
@@ -657,15 +661,16 @@ def main():
     _lib.check(lib.ae_profile_kernel(op.handle, 0, 0, 0, 1, 20, C.byref(ms_f32)))
     n0 = int(np.prod(rhs_h[0].shape[1:]))
     peak, peak_kind = measured_peaks()
-    # bytes per node the kernels must move: per-node stiffness (canonical figures) or the grain
-    # map (2-byte id per node; the per-grain table stays in L1/L2)
+    # achieved = canonical algorithmic bytes (per-node stiffness) / time; the bytes the kernels
+    # actually have to move on a grain map (2-byte id per node; the per-grain table stays in
+    # L1/L2) are reported beside them
     grains = not args.per_node_model
-    b_jac = JACOBI32_BYTES_PER_NODE_GRAINS if grains else JACOBI32_BYTES_PER_NODE
-    b_f64 = FAPPLY64_BYTES_PER_NODE_GRAINS if grains else FAPPLY64_BYTES_PER_NODE
-    b_f32 = FAPPLY32_BYTES_PER_NODE_GRAINS if grains else FAPPLY32_BYTES_PER_NODE
-    jac_gbs = b_jac * n0 / (ms_jac.value * 1e-3) / 1e9
-    fapply64_gbs = b_f64 * n0 / (ms_f64.value * 1e-3) / 1e9
-    fapply32_gbs = b_f32 * n0 / (ms_f32.value * 1e-3) / 1e9
+    a_jac = JACOBI32_BYTES_PER_NODE_GRAINS if grains else JACOBI32_BYTES_PER_NODE
+    a_f64 = FAPPLY64_BYTES_PER_NODE_GRAINS if grains else FAPPLY64_BYTES_PER_NODE
+    a_f32 = FAPPLY32_BYTES_PER_NODE_GRAINS if grains else FAPPLY32_BYTES_PER_NODE
+    jac_gbs = JACOBI32_BYTES_PER_NODE * n0 / (ms_jac.value * 1e-3) / 1e9
+    fapply64_gbs = FAPPLY64_BYTES_PER_NODE * n0 / (ms_f64.value * 1e-3) / 1e9
+    fapply32_gbs = FAPPLY32_BYTES_PER_NODE * n0 / (ms_f32.value * 1e-3) / 1e9
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -698,15 +703,17 @@ def main():
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "FP32 fused Jacobi sweep (cubic), coarse level 257^3",
                      "achieved": jac_gbs, "peak": peak, "unit": "GB/s", "frac": jac_gbs / peak,
-                     "peak_kind": peak_kind, "traffic": None,
-                     "bytes_per_node": b_jac, "ms_per_launch": ms_jac.value,
+                     "peak_kind": peak_kind, "traffic": JACOBI32_TRAFFIC_PER_NODE.get(grains, 0) * n0 or None,
+                     "traffic_source": "ncu dram bytes of the same kernel at 193^3, scaled per node",
+                     "bytes_per_node": JACOBI32_BYTES_PER_NODE, "ms_per_launch": ms_jac.value,
                      "stiffness": "grain ids + table" if grains else "per node",
-                     "canonical_bytes_per_node": JACOBI32_BYTES_PER_NODE,
-                     "canonical_gbs": JACOBI32_BYTES_PER_NODE * n0 / (ms_jac.value * 1e-3) / 1e9},
+                     "actual_bytes_per_node": a_jac,
+                     "actual_gbs": a_jac * n0 / (ms_jac.value * 1e-3) / 1e9,
+                     "actual_frac": a_jac * n0 / (ms_jac.value * 1e-3) / 1e9 / peak},
         "fapply": {"fp64_gbs": fapply64_gbs, "fp64_ms": ms_f64.value, "fp32_gbs": fapply32_gbs,
-                   "fp32_ms": ms_f32.value, "bytes_per_node_fp64": b_f64, "bytes_per_node_fp32": b_f32,
-                   "canonical_bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
-                   "canonical_bytes_per_node_fp32": FAPPLY32_BYTES_PER_NODE},
+                   "fp32_ms": ms_f32.value, "bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
+                   "bytes_per_node_fp32": FAPPLY32_BYTES_PER_NODE,
+                   "actual_bytes_per_node_fp64": a_f64, "actual_bytes_per_node_fp32": a_f32},
         "clocks": clk,
         "gpu_launches": int(launches),
         "cpu_baseline": cpu,
