@@ -94,6 +94,13 @@ struct MGLevel {
     float* gtab32 = nullptr;
     int ngrains = 0, gcap = 0;
     bool grains = false;
+    // coarsest MG level of AMR level 0: its operator as an FP64 CSR matrix, for the bottom solve
+    // of the FP32 cycle (assembled by prepare32)
+    int* csr_rowptr = nullptr;
+    int* csr_col = nullptr;
+    double* csr_val = nullptr;
+    int csr_nnz = 0, csr_cap = 0;
+    bool csr_ok = false;
 };
 
 struct AmrLevel {
@@ -302,6 +309,62 @@ void alloc_level_fp32(ae_op* op) {
     op->have32 = true;
 }
 
+// The coarsest level of AMR level 0 as an FP64 CSR matrix (levels of up to kBottomCsrMaxN
+// unknowns): dense columns A e_j on the device, compressed here, uploaded once per preparation.
+void assemble_bottom(ae_op* op) {
+    MGLevel& L = op->amr[0].mg.back();
+    L.csr_ok = false;
+    const long long N = 3 * L.nn;
+    if (N > kBottomCsrMaxN) return;
+    cudaStream_t st = op->st;
+    BottomArgs a{};
+    a.P = op->params(L.g);
+    a.K = make_scoef<double>(L.g);
+    a.C = L.C;
+    a.nn = L.nn;
+    double *A = nullptr, *E = nullptr;
+    AE_CHECK(cudaMalloc(&A, sizeof(double) * N * N));
+    cudaError_t e = cudaMalloc(&E, sizeof(double) * N * N);
+    if (e != cudaSuccess) {
+        cudaFree(A);
+        AE_CHECK(e);
+    }
+    std::vector<double> h((size_t)(N * N));
+    launch_bottom_assemble(a, A, E, st);
+    e = cudaMemcpyAsync(h.data(), A, sizeof(double) * N * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(A);
+    cudaFree(E);
+    AE_CHECK(e);
+    std::vector<int> rp((size_t)N + 1, 0), cl;
+    std::vector<double> vl;
+    for (long long r = 0; r < N; ++r) {
+        for (long long c = 0; c < N; ++c) {
+            const double v = h[(size_t)(r * N + c)];
+            if (v != 0.0) {
+                cl.push_back((int)c);
+                vl.push_back(v);
+            }
+        }
+        rp[(size_t)r + 1] = (int)cl.size();
+    }
+    const int nnz = (int)cl.size();
+    if (!L.csr_rowptr) L.csr_rowptr = op->alloc<int>(N + 1);
+    if (nnz > L.csr_cap) {
+        L.csr_col = op->alloc<int>(nnz);
+        L.csr_val = op->alloc<double>(nnz);
+        L.csr_cap = nnz;
+    }
+    AE_CHECK(cudaMemcpyAsync(L.csr_rowptr, rp.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) {
+        AE_CHECK(cudaMemcpyAsync(L.csr_col, cl.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
+        AE_CHECK(cudaMemcpyAsync(L.csr_val, vl.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    }
+    AE_CHECK(cudaStreamSynchronize(st));
+    L.csr_nnz = nnz;
+    L.csr_ok = true;
+}
+
 // FP32 copies of the stiffness and diagonal on every level (mixed-precision cycle)
 void prepare32(ae_op* op) {
     alloc_level_fp32(op);
@@ -314,6 +377,7 @@ void prepare32(ae_op* op) {
             launch_copy<float, double>(s, 3, level_view(L.g, L.invD32), cview(level_view(L.g, L.invD)), op->st);
         }
     AE_CHECK(cudaStreamSynchronize(op->st));
+    assemble_bottom(op);
     op->prepared32 = true;
 }
 
@@ -472,7 +536,9 @@ struct Cycle {
         a.sweeps = o.sweeps;
         a.omega = o.omega;
         a.fail_count = op->dflag + 1;
-        launch_bottom(a, st);
+        // the FP32 cycle's bottom: the same FP64 Krylov loop over the assembled level operator
+        if (sizeof(R) == 4 && L.csr_ok) launch_bottom_csr(a, BottomCsr{L.csr_rowptr, L.csr_col, L.csr_val, L.csr_nnz}, st);
+        else launch_bottom(a, st);
         if (sizeof(R) == 4) launch_copy<R, double>(s, 3, level_view(L.g, ptrs<R>(L).cor), cview(level_view(L.g, L.cor)), st);
     }
     void vcycle(int top) {

@@ -87,6 +87,35 @@ __device__ __forceinline__ void apply_any(const OpParams& P, const SCoef<R>& K, 
                          u.sy, u.sz, i, j, k, v);
 }
 
+// The same with the node's offsets given: oc into C (and the grain ids), ou into u
+template <int M, class R, bool GR>
+__device__ __forceinline__ void apply_at(const OpParams& P, const SCoef<R>& K, const View<const R>& C,
+                                         const Grains<R>& G, const View<const R>& u, int i, int j, int k,
+                                         long long oc, long long ou, R v[3]) {
+    if constexpr (GR)
+        apply_node_grains<M, R>(P.g, K, P.bc, P.uniform, G.gid, oc, C.sy, C.sz, G.tab, u.p, u.sc, ou, u.sy, u.sz, i,
+                                j, k, v);
+    else
+        apply_node<M, R>(P.g, K, P.bc, P.uniform, C.p, C.sc, oc, C.sy, C.sz, u.p, u.sc, ou, u.sy, u.sz, i, j, k, v);
+}
+
+// true when two views index the same storage layout (same box origin and strides): the
+// solver's level arrays all do, so one offset serves every array of a sweep
+template <class A, class B>
+inline bool same_layout(const View<A>& a, const View<B>& b) {
+    return a.lo[0] == b.lo[0] && a.lo[1] == b.lo[1] && a.lo[2] == b.lo[2] && a.sy == b.sy && a.sz == b.sz &&
+           a.sc == b.sc;
+}
+
+// Resident blocks per SM requested for the per-node sweeps.  The FP32 grain-map sweeps are
+// bound by load latency: 5 blocks of 256 threads (48 registers) hide more of it than the 4
+// (64 registers) the compiler picks by itself (257^3 Jacobi sweep 0.53 ms against 0.59 ms).
+// 0: no request (the compiler's choice).
+template <class R, bool GR>
+constexpr int sweep_min_blocks() {
+    return (sizeof(R) == 4 && GR) ? 5 : 0;
+}
+
 // ------------------------------------------------------------------ Fapply
 template <int M, class R, bool GR>
 __global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
@@ -104,24 +133,31 @@ __global__ void __launch_bounds__(kBlock) k_fapply(OpParams P, SCoef<R> K, Reg r
 }
 
 // ------------------------------------------------------------------ residual (+ norm, + FP32 copy)
-template <int M, class R, bool NORM, bool R32, bool GR>
-__global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
-                                                     View<const R> x, View<const R> b, View<R> r,
-                                                     unsigned long long* norm, View<float> r32) {
+template <int M, class R, bool NORM, bool R32, bool GR, bool SAME>
+__global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_residual(OpParams P, SCoef<R> K, Reg reg,
+                                                                                 View<const R> C, Grains<R> G,
+                                                                                 View<const R> x, View<const R> b,
+                                                                                 View<R> r, unsigned long long* norm,
+                                                                                 View<float> r32) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     double mx = 0.0;
     if (t < reg.n) {
         int i, j, k;
         reg_ijk(reg, t, i, j, k);
         R v[3];
-        apply_any<M, R, GR>(P, K, C, G, x, i, j, k, v);
-        const long long ob = b.at(i, j, k), orr = r.at(i, j, k);
+        // SAME: every view has the layout of x (checked by the launcher)
+        const long long ox = x.at(i, j, k);
+        const long long oc = SAME ? ox : C.at(i, j, k);
+        apply_at<M, R, GR>(P, K, C, G, x, i, j, k, oc, ox, v);
+        const long long ob = SAME ? ox : b.at(i, j, k), orr = SAME ? ox : r.at(i, j, k);
+        const long long o32 = SAME ? ox : (R32 ? r32.at(i, j, k) : 0);
+        const long long bsc = SAME ? x.sc : b.sc, rsc = SAME ? x.sc : r.sc, r32sc = SAME ? x.sc : r32.sc;
         const bool inv = in_box(P.g.vlo, P.g.vhi, i, j, k);
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
-            const R rv = b.p[ob + n * b.sc] - v[n];
-            r.p[orr + n * r.sc] = rv;
-            if (R32) r32.p[r32.at(i, j, k) + n * r32.sc] = (float)rv;
+            const R rv = b.p[ob + n * bsc] - v[n];
+            r.p[orr + n * rsc] = rv;
+            if (R32) r32.p[o32 + n * r32sc] = (float)rv;
             // a NaN residual reports an infinite norm (fmax alone would drop it)
             if (NORM && inv) mx = (rv != rv) ? (double)INFINITY : fmax(mx, (double)fabs(rv));
         }
@@ -131,44 +167,48 @@ __global__ void __launch_bounds__(kBlock) k_residual(OpParams P, SCoef<R> K, Reg
 
 // ------------------------------------------------------------------ damped Jacobi sweep
 // src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in.
-template <int M, class R, bool GR>
-__global__ void __launch_bounds__(kBlock) k_jacobi(OpParams P, SCoef<R> K, Reg reg, View<const R> C, Grains<R> G,
-                                                   View<const R> invD, View<const R> D, View<const R> xi,
-                                                   View<const R> b, View<R> xo, R omega) {
+template <int M, class R, bool GR, bool SAME>
+__global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_jacobi(OpParams P, SCoef<R> K, Reg reg,
+                                                                               View<const R> C, Grains<R> G,
+                                                                               View<const R> invD, View<const R> D,
+                                                                               View<const R> xi, View<const R> b,
+                                                                               View<R> xo, R omega) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= reg.n) return;
     int i, j, k;
     reg_ijk(reg, t, i, j, k);
     const Geo& g = P.g;
-    const long long ox = xi.at(i, j, k), oo = xo.at(i, j, k);
+    // SAME: every view has the layout of xi (checked by the launcher)
+    const long long ox = xi.at(i, j, k), oo = SAME ? ox : xo.at(i, j, k);
+    const long long xsc = xi.sc, osc = SAME ? xsc : xo.sc;
     // outside the domain: untouched
     if (!in_box(g.dlo, g.dhi, i, j, k)) {
 #pragma unroll
-        for (int n = 0; n < 3; ++n) xo.p[oo + n * xo.sc] = xi.p[ox + n * xi.sc];
+        for (int n = 0; n < 3; ++n) xo.p[oo + n * osc] = xi.p[ox + n * xsc];
         return;
     }
     // outermost ring of grow(valid, 2): zero
     if (g.ng >= 2 && (i == g.vlo[0] - 2 || i == g.vhi[0] + 2 || j == g.vlo[1] - 2 || j == g.vhi[1] + 2 ||
                       k == g.vlo[2] - 2 || k == g.vhi[2] + 2)) {
 #pragma unroll
-        for (int n = 0; n < 3; ++n) xo.p[oo + n * xo.sc] = R(0);
+        for (int n = 0; n < 3; ++n) xo.p[oo + n * osc] = R(0);
         return;
     }
     R v[3];
-    apply_any<M, R, GR>(P, K, C, G, xi, i, j, k, v);
-    const long long od = invD.at(i, j, k), ob = b.at(i, j, k);
+    apply_at<M, R, GR>(P, K, C, G, xi, i, j, k, SAME ? ox : C.at(i, j, k), ox, v);
+    const long long od = SAME ? ox : invD.at(i, j, k), ob = SAME ? ox : b.at(i, j, k);
+    const long long dsc = SAME ? xsc : D.sc, isc = SAME ? xsc : invD.sc, bsc = SAME ? xsc : b.sc;
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
-        const R xv = xi.p[ox + n * xi.sc];
+        const R xv = xi.p[ox + n * xsc];
         if (sizeof(R) == 8) {
             // the reference's update, (1-w) x + w (b - (Ax - D x)) / D (Operator.cpp:154)
-            const R dx = xv * D.p[od + n * D.sc];
+            const R dx = xv * D.p[od + n * dsc];
             const R rx = v[n] - dx;
-            xo.p[oo + n * xo.sc] =
-                (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
+            xo.p[oo + n * osc] = (R(1) - omega) * xv + omega * (b.p[ob + n * bsc] - rx) * invD.p[od + n * isc];
         } else {
             // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D
-            xo.p[oo + n * xo.sc] = xv + omega * (b.p[ob + n * b.sc] - v[n]) * invD.p[od + n * invD.sc];
+            xo.p[oo + n * osc] = xv + omega * (b.p[ob + n * bsc] - v[n]) * invD.p[od + n * isc];
         }
     }
 }
@@ -544,6 +584,40 @@ __global__ void __launch_bounds__(kBlock) k_fill(Reg reg, int ncomp, View<R> dst
     const long long od = dst.at(i, j, k);
     for (int n = 0; n < ncomp; ++n) dst.p[od + n * dst.sc] = value;
 }
+// Flat forms of copy / fill / axpy for a region that is the whole storage of its views (the
+// common case: level-wide vectors): the components are one contiguous run of n values, so a
+// grid-stride loop streams it with no index arithmetic.  ADD: alpha == 1, where the general form
+// dst + (Ro)(1.0 * (double)src) is exactly dst + (Ro)src (no FP64 multiply).
+template <class Ro, class Ri>
+__global__ void __launch_bounds__(kBlock) k_flat_copy(long long n, Ro* __restrict__ dst, const Ri* __restrict__ src) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = (Ro)src[t];
+}
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_flat_fill(long long n, R* __restrict__ dst, R value) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = value;
+}
+template <class Ro, class Ri, bool ADD>
+__global__ void __launch_bounds__(kBlock) k_flat_axpy(long long n, Ro* __restrict__ dst, double alpha,
+                                                      const Ri* __restrict__ src) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        if (ADD) dst[t] += (Ro)src[t];
+        else dst[t] += (Ro)(alpha * (double)src[t]);
+    }
+}
+// true when region, taken over ncomp components, is exactly the contiguous storage of v
+template <class T>
+inline bool flat_view(const Reg& reg, int ncomp, const View<T>& v) {
+    return reg.n > 0 && reg.lo[0] == v.lo[0] && reg.lo[1] == v.lo[1] && reg.lo[2] == v.lo[2] &&
+           (long long)reg.nx == v.sy && (long long)reg.nxy == v.sz && (ncomp == 1 || (long long)reg.n == v.sc);
+}
+// grid of a flat loop: enough blocks to cover n, capped at 8 resident blocks per SM of 152
+inline unsigned flat_blocks(long long n) {
+    const long long b = (n + kBlock - 1) / kBlock;
+    return (unsigned)(b < 152 * 8 ? b : 152 * 8);
+}
+
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_norminf(Reg reg, int ncomp, View<const R> v, unsigned long long* out) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;

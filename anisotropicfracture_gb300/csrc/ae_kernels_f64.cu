@@ -443,4 +443,134 @@ void launch_bottom(const BottomArgs& a, cudaStream_t st) {
     launched();
 }
 
+// ------------------------------------------------------------------ assembled bottom operator
+// The coarsest level's operator as an explicit FP64 matrix, for the bottom solve of the FP32
+// cycle.  GB300 issues FP64 at a small fraction of its FP32 rate, and the stencil form of the
+// level operator costs a few hundred FP64 instructions per node on one SM; the assembled rows
+// cost one FMA per nonzero.  Column j is the operator applied to the unit vector e_j (so every
+// entry is the stencil's own coefficient sum for that pair of unknowns); the host compresses
+// the columns to CSR.  The FP64 solve keeps the stencil form (its bottom follows the reference
+// operation for operation).
+
+// block j: column j of the dense N x N matrix A (row-major); E holds one unit vector per block
+template <int M>
+__global__ void __launch_bounds__(128) k_bottom_assemble(BottomArgs a, double* A, double* E) {
+    const long long nn = a.nn, N = 3 * nn;
+    const long long j = blockIdx.x;
+    double* e = E + j * N;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) e[t] = (t == j) ? 1.0 : 0.0;
+    __syncthreads();
+    const Geo& g = a.P.g;
+    const int nx = g.vhi[0] - g.vlo[0] + 1, ny = g.vhi[1] - g.vlo[1] + 1;
+    const long long sy = nx, sz = (long long)nx * ny;
+    for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+        const int k = (int)(t / sz), rem = (int)(t - (long long)k * sz);
+        const int jj = rem / nx, i = rem - jj * nx;
+        double v[3];
+        apply_node<M, double, true>(g, a.K, a.P.bc, a.P.uniform, a.C, nn, t, sy, sz, e, nn, t, sy, sz, i + g.vlo[0],
+                                    jj + g.vlo[1], k + g.vlo[2], v);
+        A[t * N + j] = v[0];
+        A[(t + nn) * N + j] = v[1];
+        A[(t + 2 * nn) * N + j] = v[2];
+    }
+}
+void launch_bottom_assemble(const BottomArgs& a, double* A, double* E, cudaStream_t st) {
+    dispatch_model<double>(a.P.model, [&](auto m) {
+        k_bottom_assemble<decltype(m)::value><<<(unsigned)(3 * a.nn), 128, 0, st>>>(a, A, E);
+    });
+    launched();
+}
+
+// Krylov operations over the CSR rows (one thread per row, fixed order: deterministic)
+struct CsrOps {
+    const BottomArgs& a;
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    long long N;
+    __device__ void apply(const double* x, double* out, BlkRed&) const {
+        for (long long r = threadIdx.x; r < N; r += blockDim.x) {
+            double s = 0.0;
+            for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) s += val[q] * x[col[q]];
+            out[r] = s;
+        }
+        __syncthreads();
+    }
+    __device__ void residual(const double* x, const double* b, double* r, BlkRed& sh) const {
+        apply(x, r, sh);
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) r[t] = b[t] - r[t];
+        __syncthreads();
+    }
+    __device__ double dot(const double* x, const double* y, BlkRed& sh) const {
+        double s = 0.0;
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) s += x[t] * y[t];
+        return blk_sum(s, sh);
+    }
+    __device__ double ninf(const double* x, BlkRed& sh) const {
+        double s = 0.0;
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) s = fmax(s, fabs(x[t]));
+        return blk_max(s, sh);
+    }
+    // one Fsmooth call with the level's FP64 diagonal (the same update as the stencil form)
+    __device__ void smooth(double* x, const double* b, double* tmp, BlkRed& sh) const {
+        for (int s = 0; s < a.sweeps; ++s) {
+            apply(x, tmp, sh);
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                const double xv = x[t];
+                const double rx = tmp[t] - xv * a.D[t];
+                x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * a.invD[t];
+            }
+            __syncthreads();
+        }
+    }
+};
+
+// the matrix and the vectors in dynamic shared memory when they fit (SMEM), else from global
+template <bool SMEM>
+__global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, BottomCsr m) {
+    __shared__ BlkRed sh;
+    extern __shared__ double smem[];
+    const long long N = 3 * a.nn;
+    double* x = a.x;
+    const double* b = a.b;
+    double* work = a.work;
+    const int* rowptr = m.rowptr;
+    const int* col = m.col;
+    const double* val = m.val;
+    if (SMEM) {
+        double* sval = smem;
+        double* sb = sval + m.nnz;
+        double* sx = sb + N;
+        double* sw = sx + N;
+        int* srow = reinterpret_cast<int*>(sw + 8 * N);
+        int* scol = srow + N + 1;
+        for (long long t = threadIdx.x; t < m.nnz; t += blockDim.x) { sval[t] = m.val[t]; scol[t] = m.col[t]; }
+        for (long long t = threadIdx.x; t <= N; t += blockDim.x) srow[t] = m.rowptr[t];
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) { sb[t] = a.b[t]; sx[t] = a.x[t]; }
+        __syncthreads();
+        rowptr = srow; col = scol; val = sval; b = sb; x = sx; work = sw;
+    }
+    const CsrOps ops{a, rowptr, col, val, N};
+    const KrylovParams kp{a.bottom, a.maxiter, a.reltol, a.nuf};
+    const int ret = krylov_bottom(ops, kp, N, x, b, work, sh);
+    if (ret != 0 && ret != 9 && threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
+    if (SMEM) {
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
+    }
+}
+
+size_t bottom_csr_smem_bytes(long long N, long long nnz) {
+    return (size_t)(nnz + 10 * N) * sizeof(double) + (size_t)(N + 1 + nnz) * sizeof(int);
+}
+
+// one thread per row, rounded up to whole warps
+void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st) {
+    const long long N = 3 * a.nn;
+    const int threads = (int)std::min<long long>(kBottomThreads, (N + 31) / 32 * 32);
+    const size_t bytes = bottom_csr_smem_bytes(N, m.nnz);
+    if (bytes <= kBottomSmemBytes) k_bottom_csr<true><<<1, threads, bytes, st>>>(a, m);
+    else k_bottom_csr<false><<<1, threads, 0, st>>>(a, m);
+    launched();
+}
+
 }  // namespace ae

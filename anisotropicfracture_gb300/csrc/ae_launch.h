@@ -182,5 +182,18 @@ struct BottomArgs {
     int* fail_count;  // incremented when the Krylov solve fails
 };
 void launch_bottom(const BottomArgs& a, cudaStream_t st);
+// Coarsest-level operator assembled as an FP64 CSR matrix (rows = unknowns t + c nn), used by the
+// bottom solve of the FP32 cycle.  The dense form comes first: column j of the row-major N x N
+// matrix A is the operator applied to e_j (E: N x N scratch for the unit vectors).
+struct BottomCsr {
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    int nnz;
+};
+void launch_bottom_assemble(const BottomArgs& a, double* A, double* E, cudaStream_t st);
+void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st);
+// unknowns up to which the coarsest level is assembled (dense scratch 2 N^2 doubles at set-up)
+constexpr long long kBottomCsrMaxN = 1536;
 
 }  // namespace ae

@@ -50,9 +50,9 @@ JACOBI32_BYTES_PER_NODE_GRAINS = 12 + 12 + 12 + 2 + 12
 FAPPLY64_BYTES_PER_NODE_GRAINS = 24 + 2 + 24
 FAPPLY32_BYTES_PER_NODE_GRAINS = 12 + 2 + 12
 # measured DRAM bytes per node of the FP32 Jacobi sweep (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum at 193^3, larger than L2; profiles/jacobi32_dram_193cubed.md), keyed by
-# grain map on/off; 0 = not measured
-JACOBI32_TRAFFIC_PER_NODE = {True: 0, False: 0}
+# dram__bytes_write.sum at 193^3, larger than L2, mean of two launches;
+# profiles/jacobi32_dram_193cubed.md), keyed by grain map on/off
+JACOBI32_TRAFFIC_PER_NODE = {True: 47.3, False: 131.1}
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
 # time to a full solve in the reference arm, which cannot afford a full CPU solve.
@@ -602,8 +602,12 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         st = None
+        # NVTX range "timed_<prec>": ncu --nvtx --nvtx-include "timed_mixed/" lists exactly the
+        # launches of the timed solves
+        torch.cuda.nvtx.range_push("timed_" + prec)
         for _ in range(steps):
             st = solve_device(prec)
+        torch.cuda.nvtx.range_pop()
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
