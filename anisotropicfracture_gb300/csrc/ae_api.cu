@@ -727,6 +727,11 @@ void iteration_body(ae_op* op, const ae_solver_opts& o, bool fcyc) {
             for (int a = 0; a <= it.finest(); ++a)
                 launch_axpy<double, float>(it.store_dom(a), 3, level_view(it.G(a), op->amr[a].sol), 1.0,
                                            it.CV(a, e[a]), st);
+            // the patches' outermost ghost rings: the coarse correction interpolated in FP64, as
+            // the FP64 solve's rings hold (see k_ring_interp_fix)
+            for (int a = 1; a <= it.finest(); ++a)
+                launch_ring_interp_fix(it.G(a), level_view(it.G(a), op->amr[a].sol), it.CV(a - 1, e[a - 1]),
+                                       it.CV(a, e[a]), st);
             AmrIter<double> it64{op, o, st, sol64(op), rhs64(op)};
             for (int a = it.finest(); a >= 1; --a) it64.average_down(a);
         }

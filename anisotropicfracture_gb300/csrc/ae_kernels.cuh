@@ -520,29 +520,31 @@ __global__ void __launch_bounds__(kBlock) k_restrict(Geo gc, Reg reg, int ncomp,
     }
 }
 
-// src/Operator/Operator.cpp:589-618 (fine node (i,j,k), coarse node (i/2, j/2, k/2))
+// src/Operator/Operator.cpp:589-618 (fine node (i,j,k), coarse node (i/2, j/2, k/2)): the
+// coarse field interpolated to fine node (i, j, k), component n, in the arithmetic type T
+template <class T, class R>
+__device__ __forceinline__ T interp_at(const View<const R>& crse, int i, int j, int k, int n) {
+    const int I = i >> 1, J = j >> 1, Kc = k >> 1;  // non-negative indices
+    const bool ie = !(i & 1), je = !(j & 1), ke = !(k & 1);
+    const long long sy = crse.sy, sz = crse.sz;
+    const R* c = crse.p + crse.at(I, J, Kc) + n * crse.sc;
+    const auto C = [&](long long o) { return (T)c[o]; };
+    if (ie && je && ke) return C(0);
+    if (je && ke) return T(0.5) * (C(0) + C(1));
+    if (ke && ie) return T(0.5) * (C(0) + C(sy));
+    if (ie && je) return T(0.5) * (C(0) + C(sz));
+    if (ie) return T(0.25) * (C(0) + C(sy) + C(sz) + C(sy + sz));
+    if (je) return T(0.25) * (C(0) + C(sz) + C(1) + C(1 + sz));
+    if (ke) return T(0.25) * (C(0) + C(1) + C(sy) + C(1 + sy));
+    return T(0.125) * (C(0) + C(1) + C(sy) + C(sz) + C(sy + sz) + C(1 + sz) + C(1 + sy) + C(1 + sy + sz));
+}
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_interp_add(Reg reg, int ncomp, View<R> fine, View<const R> crse) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= reg.n) return;
     int i, j, k;
     reg_ijk(reg, t, i, j, k);
-    const int I = i >> 1, J = j >> 1, Kc = k >> 1;  // non-negative indices
-    const bool ie = !(i & 1), je = !(j & 1), ke = !(k & 1);
-    const long long sy = crse.sy, sz = crse.sz;
-    for (int n = 0; n < ncomp; ++n) {
-        const R* c = crse.p + crse.at(I, J, Kc) + n * crse.sc;
-        R v;
-        if (ie && je && ke) v = c[0];
-        else if (je && ke) v = R(0.5) * (c[0] + c[1]);
-        else if (ke && ie) v = R(0.5) * (c[0] + c[sy]);
-        else if (ie && je) v = R(0.5) * (c[0] + c[sz]);
-        else if (ie) v = R(0.25) * (c[0] + c[sy] + c[sz] + c[sy + sz]);
-        else if (je) v = R(0.25) * (c[0] + c[sz] + c[1] + c[1 + sz]);
-        else if (ke) v = R(0.25) * (c[0] + c[1] + c[sy] + c[1 + sy]);
-        else v = R(0.125) * (c[0] + c[1] + c[sy] + c[sz] + c[sy + sz] + c[1 + sz] + c[1 + sy] + c[1 + sy + sz]);
-        fine.p[fine.at(i, j, k) + n * fine.sc] += v;
-    }
+    for (int n = 0; n < ncomp; ++n) fine.p[fine.at(i, j, k) + n * fine.sc] += interp_at<R, R>(crse, i, j, k, n);
 }
 
 // nodal average_down (src/Operator/Operator.cpp:631): coarse node I takes fine node 2I

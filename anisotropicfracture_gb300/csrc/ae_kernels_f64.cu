@@ -443,6 +443,37 @@ void launch_bottom(const BottomArgs& a, cudaStream_t st) {
     launched();
 }
 
+// Mixed precision on a refined patch: the FP32 correction e was just added to the FP64 solution
+// x.  The outermost ghost ring of the patch (grow(valid, 2)) has no equation of its own; in the
+// FP64 solve it only ever receives coarse corrections interpolated to it, so there it equals the
+// interpolation of the coarse solution.  The FP32 cycle interpolates in FP32, and its rounding
+// would stay in the ring (nothing corrects it) and bias the interface rows.  Here the ring's
+// increment is replaced by the coarse FP32 correction interpolated in FP64:
+//   x_ring += interp(e_coarse) - e_ring.
+__global__ void __launch_bounds__(kBlock) k_ring_interp_fix(Reg reg, Geo gf, View<double> x, View<const float> ecrse,
+                                                            View<const float> efine) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const bool ring = i == gf.vlo[0] - 2 || i == gf.vhi[0] + 2 || j == gf.vlo[1] - 2 || j == gf.vhi[1] + 2 ||
+                      k == gf.vlo[2] - 2 || k == gf.vhi[2] + 2;
+    if (!ring) return;
+    for (int n = 0; n < 3; ++n) {
+        const double v = interp_at<double, float>(ecrse, i, j, k, n);
+        x.p[x.at(i, j, k) + n * x.sc] += v - (double)efine.p[efine.at(i, j, k) + n * efine.sc];
+    }
+}
+
+void launch_ring_interp_fix(const Geo& gf, View<double> x, View<const float> ecrse, View<const float> efine,
+                            cudaStream_t st) {
+    if (gf.ng < 2) return;
+    const Reg reg = make_reg(box_isect(geo_store(gf), geo_domain(gf)));
+    if (reg.n == 0) return;
+    k_ring_interp_fix<<<nblocks(reg.n), kBlock, 0, st>>>(reg, gf, x, ecrse, efine);
+    launched();
+}
+
 // ------------------------------------------------------------------ assembled bottom operator
 // The coarsest level's operator as an explicit FP64 matrix, for the bottom solve of the FP32
 // cycle.  GB300 issues FP64 at a small fraction of its FP32 rate, and the stencil form of the

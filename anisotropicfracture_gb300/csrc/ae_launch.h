@@ -182,6 +182,10 @@ struct BottomArgs {
     int* fail_count;  // incremented when the Krylov solve fails
 };
 void launch_bottom(const BottomArgs& a, cudaStream_t st);
+// mixed precision, refined patch gf (ghost layers >= 2): on the outermost ghost ring replace the
+// FP32 correction just added to x by the coarse correction interpolated in FP64
+void launch_ring_interp_fix(const Geo& gf, View<double> x, View<const float> ecrse, View<const float> efine,
+                            cudaStream_t st);
 // Coarsest-level operator assembled as an FP64 CSR matrix (rows = unknowns t + c nn), used by the
 // bottom solve of the FP32 cycle.  The dense form comes first: column j of the row-major N x N
 // matrix A is the operator applied to e_j (E: N x N scratch for the unit vectors).

@@ -523,6 +523,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--oracle-tol", type=float, default=1e-9,
                     help="residual of the FP64 oracle solution the displacement errors are measured against (0: off)")
+    ap.add_argument("--path-check", action="store_true",
+                    help="also solve in FP64 with F-cycles and report its distance to the oracle solution")
     ap.add_argument("--mixed-tight-tol", type=float, default=0.0,
                     help="also time the mixed solve to this residual and report its error (0: off)")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -719,6 +721,20 @@ def main():
                   "per_level_mixed": where(x_mixed),
                   "displacement_err_mixed_incl_ghosts": ghost_err,
                   "measured_on": "valid nodes of both levels (the composite solution)"}
+        # another FP64 iteration path (F-cycles) to the same 1e-8 residual: how far two FP64 paths
+        # land apart measures the non-uniqueness of the composite solution on its own
+        if args.path_check:
+            solver.setPrecision("fp64")
+            solver.setMaxFmgIter(1 << 30)
+            with torch.cuda.stream(stream):
+                for x in sol_d:
+                    x.zero_()
+            xs3, rs3 = fields(sol_d, rhs_d)
+            solver.solve(xs3, rs3, 1e-8, 0.0)
+            solver.setMaxFmgIter(0)
+            x_f = [x.cpu().numpy() for x in sol_d]
+            oracle["fp64_fcycle"] = {"iters": solver.stats.iters, "displacement_err": err_vs_oracle(x_f),
+                                     "displacement_err_away_from_interface": away(x_f)}
         # the mixed solve to a tighter residual, timed the same way, with its error
         if args.mixed_tight_tol > 0:
             def solve_tight():
