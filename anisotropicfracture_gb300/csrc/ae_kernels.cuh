@@ -111,9 +111,12 @@ inline bool same_layout(const View<A>& a, const View<B>& b) {
 // bound by load latency: 5 blocks of 256 threads (48 registers) hide more of it than the 4
 // (64 registers) the compiler picks by itself (257^3 Jacobi sweep 0.53 ms against 0.59 ms).
 // 0: no request (the compiler's choice).
+#ifndef AE_GRAIN_SWEEP_BLOCKS
+#define AE_GRAIN_SWEEP_BLOCKS 5
+#endif
 template <class R, bool GR>
 constexpr int sweep_min_blocks() {
-    return (sizeof(R) == 4 && GR) ? 5 : 0;
+    return (sizeof(R) == 4 && GR) ? AE_GRAIN_SWEEP_BLOCKS : 0;
 }
 
 // ------------------------------------------------------------------ Fapply

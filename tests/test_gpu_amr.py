@@ -74,6 +74,28 @@ def test_amr_polycrystal_mixed_error():
     assert max(np.abs(x - r).max() for x, r in zip(xs, ref)) / scale < 1e-7
 
 
+@pytest.mark.parametrize("nlev", [2, 3])
+def test_amr_mixed_lands_on_the_fp64_solution(nlev):
+    """The mixed solve of a refined hierarchy converges to the FP64 solve's composite solution, not
+    just to the same residual.  The patches' outermost ghost ring has no equation: the FP64 solve
+    fills it with interpolated coarse corrections, and the mixed solve must do the same in FP64
+    (k_ring_interp_fix); with the FP32 interpolation's rounding left there, the interface rows
+    were biased and the two solutions sat about 1e-7 apart.  Both solves go to 1e-10 here, so
+    the distance on the valid nodes must be at that level."""
+    Ls, Cs, bc, bs = polycrystal_amr(16, nlev)
+    x64, s64 = gpu_amr_solve(Ls, models.MAJORMINOR, Cs, bc, bs, precision="fp64", tol=1e-10)
+    xm, sm = gpu_amr_solve(Ls, models.MAJORMINOR, Cs, bc, bs, precision="mixed", tol=1e-10)
+    assert s64.converged and sm.converged
+
+    def valid(L, a):
+        g = L.ng
+        return a if g == 0 else a[:, g:-g, g:-g, g:-g]
+
+    scale = max(np.abs(valid(L, r)).max() for L, r in zip(Ls, x64))
+    err = max(np.abs(valid(L, a) - valid(L, b)).max() for L, a, b in zip(Ls, xm, x64)) / scale
+    assert err < 1e-9, err
+
+
 def test_amr_trig_known_answer_on_gpu():
     n, nlev = 32, 2
     Ls = po.amr_levels(n, nlev)
