@@ -286,7 +286,10 @@ void ae_server_default_opts(ae_server_opts* o) {
     o->solver.max_fmg_iter = 0;
     o->solver.bottom = 1;
     o->solver.precision = 1;
-    o->solver.inner_cycles = 2;
+    // FP32 cycles per FP64 residual: the FP64 residual of a cell batch costs about a third of
+    // an FP32 V-cycle on GB300, so 4 (512-cell batch: 443 solves/s, against 396 with 2;
+    // displacement error 4.6e-8 against FP64)
+    o->solver.inner_cycles = 4;
     o->solver.use_graph = 1;
 }
 

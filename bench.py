@@ -380,6 +380,16 @@ def _barrier(world):
         dist.barrier()
 
 
+def _nvtx_push(name):
+    import torch
+    torch.cuda.nvtx.range_push(name)
+
+
+def _nvtx_pop():
+    import torch
+    torch.cuda.nvtx.range_pop()
+
+
 def bench_batch(args, lib, rank=0, world=1):
     """Batched cells: mixed and FP64 in one batch, FP64 one cell at a time, CPU oracle sample.
     With N ranks each takes its largest-first share of the cells (no collective on the data path)
@@ -410,8 +420,10 @@ def bench_batch(args, lib, rank=0, world=1):
         _barrier(world)
         t0 = time.perf_counter()
         reps = max(1, args.batch_steps)
+        _nvtx_push("batch_" + name)  # ncu --nvtx --nvtx-include "batch_mixed/" lists the timed launches
         for _ in range(reps):
             st, rc = B.solve(precision=prec, inner_cycles=args.batch_inner, check=False, **CELL_SOLVER)
+        _nvtx_pop()
         secs = _max_over_ranks((time.perf_counter() - t0) / reps, world)
         launches = (lib.ae_kernel_launches() - l0) // reps
         res[name] = {"value": total / secs, "s_per_batch": secs, "converged": rc == 0,
@@ -544,7 +556,8 @@ def main():
     ap.add_argument("--only-cells", action="store_true", help="run only the batched/served cell workloads")
     ap.add_argument("--batch-cells", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2)
-    ap.add_argument("--batch-inner", type=int, default=2)
+    ap.add_argument("--batch-inner", type=int, default=4,
+                    help="FP32 cycles per FP64 residual for the batched and served cells")
     ap.add_argument("--batch-single-limit", type=int, default=0, help="cells timed one at a time (0: all)")
     ap.add_argument("--batch-cpu-sample", type=int, default=4)
     ap.add_argument("--serve-requests", type=int, default=24)

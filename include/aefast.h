@@ -315,7 +315,7 @@ typedef struct {
 
 typedef struct ae_server_s* ae_server;
 
-void ae_server_default_opts(ae_server_opts* opts);  /* mixed precision, 2 inner cycles, 1e-8, graphs */
+void ae_server_default_opts(ae_server_opts* opts);  /* mixed precision, 4 inner cycles, 1e-8, graphs */
 int ae_server_create(int model, const ae_server_opts* opts, ae_server* out);
 /* Stop the worker (finishing its current iteration) and free everything; queued and running
  * requests are dropped. */
