@@ -205,6 +205,32 @@ def cpu_oracle_sample(levels, bc, n_iters_solve, sample_iters=1, threads=None, r
                        % (t_setup, sample_iters, t_iter, n_iters_solve))
 
 
+def cpu_single_thread(levels, bc, cpu):
+    """The same solve on one host thread (the reference's per-rank Fapply/Fsmooth are
+    single-threaded), estimated from the oracle's Fapply on the coarse level timed at one thread
+    and at all threads: one solve at one thread ~ the all-thread solve x that ratio."""
+    from oracle import pyoracle as po
+    L = levels[0]
+    Lo = oracle_level(L)
+    u = np.random.default_rng(0).standard_normal((3,) + level_shape(L))
+    nthreads = po.lib().orc_num_threads()
+
+    def t_apply(threads):
+        po.set_threads(threads)
+        po.fapply(Lo, po.ORC_MAJORMINOR, L["C"], bc.type, u)  # warm
+        t0 = time.perf_counter()
+        po.fapply(Lo, po.ORC_MAJORMINOR, L["C"], bc.type, u)
+        return time.perf_counter() - t0
+
+    t1 = t_apply(1)
+    tn = t_apply(nthreads)
+    po.set_threads(nthreads)
+    ratio = t1 / tn
+    return {"value": cpu["value"] / ratio, "unit": UNIT, "cores": 1,
+            "sample": "all-thread oracle solve time x the Fapply time ratio 1 thread / %d threads on the "
+                      "%d^3-node coarse level (%.2f s / %.3f s = %.1f)" % (nthreads, L["cells"] + 1, t1, tn, ratio)}
+
+
 def run_reference(args, rank):
     """Reference arm: the reference's CPU path (its C++ restatement in oracle/, the reference
     itself needs AMReX/Eigen/MPI, absent here) timed on the host cores."""
@@ -815,6 +841,7 @@ def main():
         try:
             cpu = cpu_oracle_sample(levels, bc, fp64_iters or iters_mixed, sample_iters=args.cpu_sample_iters,
                                     rhs=rhs_h)
+            cpu["single_thread"] = cpu_single_thread(levels, bc, cpu)
         except Exception as e:  # pragma: no cover
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: %s" % e}
 
