@@ -279,9 +279,9 @@ def bench_config2(args):
     for f in FACES:
         if "ZHI" in f:
             bc.Set(f, 2, bc.Displacement, 0.005)
+    C = np.ascontiguousarray(C)
     op = Elastic([level_desc(n)], models.MAJORMINOR)
-    op.SetModel(0, Field(np.ascontiguousarray(C)))
-    del C
+    op.SetModel(0, Field(C))
     op.SetBC(bc)
     op.SetUniform(False)
     op.prepareForSolve()
@@ -315,6 +315,28 @@ def bench_config2(args):
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["displacement_err_mixed_vs_fp64"] = float(np.abs(xs["mixed"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
     op.close()
+    if not args.no_cpu:
+        # the FP64 oracle on the host cores: set-up plus one V-cycle, extrapolated to the
+        # iterations of the GPU FP64 solve (the same algorithm)
+        try:
+            from oracle import pyoracle as po
+            L = po.level(n)
+            bh = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
+            kw = dict(max_fmg_iter=0, bottom=0, nu1=2, nu2=2)
+            t0 = time.perf_counter()
+            po.solve(L, po.ORC_MAJORMINOR, C, bc.type, np.zeros_like(bh), bh, 1e-30, 0.0, max_iter=0, **kw)
+            t_setup = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            po.solve(L, po.ORC_MAJORMINOR, C, bc.type, np.zeros_like(bh), bh, 1e-30, 0.0, max_iter=1, **kw)
+            t_iter = max(time.perf_counter() - t0 - t_setup, 1e-9)
+            iters = out["fp64"]["iters"]
+            out["cpu_baseline"] = {"value": 1.0 / (t_setup + iters * t_iter), "unit": UNIT,
+                                   "cores": po.lib().orc_num_threads(), "kind": "port",
+                                   "sample": "FP64 oracle, set-up %.1f s + 1 V-cycle at %.2f s, extrapolated to the "
+                                             "%d cycles of the FP64 solve" % (t_setup, t_iter, iters)}
+        except Exception as e:  # pragma: no cover
+            out["cpu_baseline"] = {"value": None, "sample": "failed: %s" % e}
+    del C
     return out
 
 
