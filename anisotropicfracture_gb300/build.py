@@ -27,9 +27,13 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
+# extra nvcc flags (e.g. "-DAE_GRAIN_SWEEP_BLOCKS=4" to try another resident-block count)
+EXTRA = os.environ.get("AE_NVCC_FLAGS", "").split()
+
+
 def _compile(src):
     obj = os.path.join(OBJ, src.replace(".cu", ".o"))
-    cmd = [NVCC] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [NVCC] + ARCH + FLAGS + EXTRA + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))

@@ -59,11 +59,27 @@ __device__ __forceinline__ void level_apply(const CellLevelDev& L, int uniform, 
 }
 
 constexpr int kCellThreads = 256;
+// Resident blocks per SM requested for the FP32 cell sweeps (smoother, correction residual);
+// 0: the compiler's choice.  On a 512-cell mixed batch:
+//   finest level on a grain map: 4 blocks (64 registers), 482 solves/s, against 444 with the
+//     compiler's 80 registers;
+//   per-node levels: 3 blocks (80 registers, about 100 B of spills), 507 solves/s, against 482
+//     with the compiler's 118 registers.
+#ifndef AE_CELL_SMOOTH_BLOCKS
+#define AE_CELL_SMOOTH_BLOCKS 4
+#endif
+#ifndef AE_CELL_SMOOTH_BLOCKS_PERNODE
+#define AE_CELL_SMOOTH_BLOCKS_PERNODE 3
+#endif
+template <class R, bool GR>
+constexpr int cell_min_blocks() {
+    return sizeof(R) != 4 ? 0 : GR ? AE_CELL_SMOOTH_BLOCKS : AE_CELL_SMOOTH_BLOCKS_PERNODE;
+}
 
 // one damped-Jacobi sweep of the correction at level m: from2 = 0 reads cor and writes cor2,
 // from2 = 1 the reverse.  ZERO: the input is the zero vector (the first sweep of a V-cycle).
 template <int M, class R, bool ZERO, bool GR>
-__global__ void __launch_bounds__(kCellThreads) kb_smooth(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
+__global__ void __launch_bounds__(kCellThreads, cell_min_blocks<R, GR>()) kb_smooth(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
                                                           int from2) {
     for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
         const Work w = tab[e];
@@ -127,7 +143,7 @@ __global__ void __launch_bounds__(kCellThreads) kb_copy2(CellArgs A, const Work*
 
 // rescor = res - A cor at level m (inplace: into res)
 template <int M, class R, bool GR>
-__global__ void __launch_bounds__(kCellThreads) kb_rescor(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
+__global__ void __launch_bounds__(kCellThreads, cell_min_blocks<R, GR>()) kb_rescor(CellArgs A, const Work* __restrict__ tab, int ntab, int m,
                                                           int inplace) {
     for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
         const Work w = tab[e];
