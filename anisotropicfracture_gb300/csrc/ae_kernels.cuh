@@ -550,6 +550,39 @@ __global__ void __launch_bounds__(kBlock) k_interp_add(Reg reg, int ncomp, View<
     for (int n = 0; n < ncomp; ++n) fine.p[fine.at(i, j, k) + n * fine.sc] += interp_at<R, R>(crse, i, j, k, n);
 }
 
+// The same interpolation, one thread per coarse node (I, J, K) of the coarse box cb: it adds into
+// the up to 8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, that lie in the fine region
+// [flo, fhi].  The parity of each of those nodes is known at compile time, so a warp runs no
+// divergent branches and the coarse values are loaded once for the 8 nodes.  Each node's value
+// is formed by the same expression as in k_interp_add.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_interp_add8(Reg cb, Box3 fr, int ncomp, View<R> fine,
+                                                        View<const R> crse) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cb.n) return;
+    int I, J, Kc;
+    reg_ijk(cb, t, I, J, Kc);
+    const long long sy = crse.sy, sz = crse.sz;
+    const bool x1 = 2 * I + 1 <= fr.hi[0], y1 = 2 * J + 1 <= fr.hi[1], z1 = 2 * Kc + 1 <= fr.hi[2];
+    const bool x0 = 2 * I >= fr.lo[0], y0 = 2 * J >= fr.lo[1], z0 = 2 * Kc >= fr.lo[2];
+    for (int n = 0; n < ncomp; ++n) {
+        const R* __restrict__ c = crse.p + crse.at(I, J, Kc) + n * crse.sc;
+        R* __restrict__ f = fine.p + fine.at(2 * I, 2 * J, 2 * Kc) + n * fine.sc;
+        const long long fy = fine.sy, fz = fine.sz;
+        // (a, b, c) = (0, 0, 0): the coincident node
+        if (x0 && y0 && z0) f[0] += c[0];
+        if (x1 && y0 && z0) f[1] += R(0.5) * (c[0] + c[1]);
+        if (x0 && y1 && z0) f[fy] += R(0.5) * (c[0] + c[sy]);
+        if (x0 && y0 && z1) f[fz] += R(0.5) * (c[0] + c[sz]);
+        if (x0 && y1 && z1) f[fy + fz] += R(0.25) * (c[0] + c[sy] + c[sz] + c[sy + sz]);
+        if (x1 && y0 && z1) f[1 + fz] += R(0.25) * (c[0] + c[sz] + c[1] + c[1 + sz]);
+        if (x1 && y1 && z0) f[1 + fy] += R(0.25) * (c[0] + c[1] + c[sy] + c[1 + sy]);
+        if (x1 && y1 && z1)
+            f[1 + fy + fz] +=
+                R(0.125) * (c[0] + c[1] + c[sy] + c[sz] + c[sy + sz] + c[1 + sz] + c[1 + sy] + c[1 + sy + sz]);
+    }
+}
+
 // nodal average_down (src/Operator/Operator.cpp:631): coarse node I takes fine node 2I
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_inject(Reg reg, int ncomp, View<R> crse, View<const R> fine) {
