@@ -541,20 +541,12 @@ __device__ __forceinline__ T interp_at(const View<const R>& crse, int i, int j, 
     if (ke) return T(0.25) * (C(0) + C(1) + C(sy) + C(1 + sy));
     return T(0.125) * (C(0) + C(1) + C(sy) + C(sz) + C(sy + sz) + C(1 + sz) + C(1 + sy) + C(1 + sy + sz));
 }
-template <class R>
-__global__ void __launch_bounds__(kBlock) k_interp_add(Reg reg, int ncomp, View<R> fine, View<const R> crse) {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= reg.n) return;
-    int i, j, k;
-    reg_ijk(reg, t, i, j, k);
-    for (int n = 0; n < ncomp; ++n) fine.p[fine.at(i, j, k) + n * fine.sc] += interp_at<R, R>(crse, i, j, k, n);
-}
-
-// The same interpolation, one thread per coarse node (I, J, K) of the coarse box cb: it adds into
+// Interpolation added into the fine level, one thread per coarse node (I, J, K) of the coarse box
+// cb: it adds into
 // the up to 8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, that lie in the fine region
 // [flo, fhi].  The parity of each of those nodes is known at compile time, so a warp runs no
 // divergent branches and the coarse values are loaded once for the 8 nodes.  Each node's value
-// is formed by the same expression as in k_interp_add.
+// is the expression of interp_at for its parity.
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_interp_add8(Reg cb, Box3 fr, int ncomp, View<R> fine,
                                                         View<const R> crse) {
