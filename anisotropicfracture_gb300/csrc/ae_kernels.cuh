@@ -541,12 +541,12 @@ __device__ __forceinline__ T interp_at(const View<const R>& crse, int i, int j, 
     if (ke) return T(0.25) * (C(0) + C(1) + C(sy) + C(1 + sy));
     return T(0.125) * (C(0) + C(1) + C(sy) + C(sz) + C(sy + sz) + C(1 + sz) + C(1 + sy) + C(1 + sy + sz));
 }
-// Interpolation added into the fine level, one thread per coarse node (I, J, K) of the coarse box
-// cb: it adds into
-// the up to 8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, that lie in the fine region
-// [flo, fhi].  The parity of each of those nodes is known at compile time, so a warp runs no
-// divergent branches and the coarse values are loaded once for the 8 nodes.  Each node's value
-// is the expression of interp_at for its parity.
+
+// Interpolation added into the fine level (the same weights), one thread per coarse node
+// (I, J, K) of the coarse box cb: it adds into the up to 8 fine nodes (2I + a, 2J + b, 2K + c),
+// a, b, c in {0, 1}, that lie in the fine region fr.  The parity of each of those nodes is known
+// at compile time, so a warp runs no divergent branches and the coarse values are loaded once
+// for the 8 nodes.  Each node's value is the expression of interp_at for its parity.
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_interp_add8(Reg cb, Box3 fr, int ncomp, View<R> fine,
                                                         View<const R> crse) {
