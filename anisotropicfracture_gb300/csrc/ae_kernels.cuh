@@ -114,9 +114,12 @@ inline bool same_layout(const View<A>& a, const View<B>& b) {
 #ifndef AE_GRAIN_SWEEP_BLOCKS
 #define AE_GRAIN_SWEEP_BLOCKS 5
 #endif
+#ifndef AE_PERNODE_SWEEP_BLOCKS
+#define AE_PERNODE_SWEEP_BLOCKS 0
+#endif
 template <class R, bool GR>
 constexpr int sweep_min_blocks() {
-    return (sizeof(R) == 4 && GR) ? AE_GRAIN_SWEEP_BLOCKS : 0;
+    return sizeof(R) != 4 ? 0 : GR ? AE_GRAIN_SWEEP_BLOCKS : AE_PERNODE_SWEEP_BLOCKS;
 }
 
 // ------------------------------------------------------------------ Fapply
