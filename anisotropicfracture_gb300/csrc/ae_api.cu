@@ -322,20 +322,19 @@ void assemble_bottom(ae_op* op) {
     a.K = make_scoef<double>(L.g);
     a.C = L.C;
     a.nn = L.nn;
-    double *A = nullptr, *E = nullptr;
-    AE_CHECK(cudaMalloc(&A, sizeof(double) * N * N));
-    cudaError_t e = cudaMalloc(&E, sizeof(double) * N * N);
-    if (e != cudaSuccess) {
-        cudaFree(A);
-        AE_CHECK(e);
-    }
+    // the dense matrix and the unit vectors live only for the assembly (freed on every path)
+    struct Scratch {
+        double* p = nullptr;
+        ~Scratch() {
+            if (p) cudaFree(p);
+        }
+    } A, E;
+    AE_CHECK(cudaMalloc(&A.p, sizeof(double) * N * N));
+    AE_CHECK(cudaMalloc(&E.p, sizeof(double) * N * N));
     std::vector<double> h((size_t)(N * N));
-    launch_bottom_assemble(a, A, E, st);
-    e = cudaMemcpyAsync(h.data(), A, sizeof(double) * N * N, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(A);
-    cudaFree(E);
-    AE_CHECK(e);
+    launch_bottom_assemble(a, A.p, E.p, st);
+    AE_CHECK(cudaMemcpyAsync(h.data(), A.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, st));
+    AE_CHECK(cudaStreamSynchronize(st));
     std::vector<int> rp((size_t)N + 1, 0), cl;
     std::vector<double> vl;
     for (long long r = 0; r < N; ++r) {
