@@ -75,3 +75,23 @@ def normwise_err(a, ref):
     """max |a - ref| / max |ref|: the per-node error measured against the field's scale."""
     s = np.abs(ref).max()
     return float(np.abs(a - ref).max() / (s if s > 0 else 1.0))
+
+
+def polycrystal_amr(n=16, nlev=2, seed=1):
+    """The reference's test hierarchy (oracle amr_levels) with an 8-grain cubic Voronoi stiffness
+    on every level (ghost nodes included) and the config-0 boundary values as right-hand sides."""
+    from anisotropicfracture_gb300 import microstructure
+    from oracle import pyoracle as po
+    Ls = po.amr_levels(n, nlev)
+    bc = bc_config0()
+    seeds = microstructure.voronoi_seeds(8, seed)
+    rot = models.random_rotations(8, np.random.default_rng(seed + 1))
+    tab = models.cubic(1.68, 1.21, 0.75, rot)
+    Cs, bs = [], []
+    for L in Ls:
+        lo = [L.lo[d] - L.ng for d in range(3)]
+        hi = [L.hi[d] + L.ng for d in range(3)]
+        gid = microstructure.voronoi_grain_ids(lo, hi, tuple(L.dx), seeds)
+        Cs.append(np.ascontiguousarray(np.moveaxis(tab[gid], -1, 0)))
+        bs.append(po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)))
+    return Ls, Cs, bc, bs

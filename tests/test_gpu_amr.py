@@ -2,9 +2,9 @@
 import numpy as np
 import pytest
 
-from anisotropicfracture_gb300 import microstructure, models
+from anisotropicfracture_gb300 import models
 from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
-from helpers import bc_config0, normwise_err
+from helpers import polycrystal_amr
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
@@ -36,22 +36,6 @@ def gpu_amr_solve(Ls, model, Cs, bc, bs, precision="fp64", fmg=0, bottom=0, nu=1
     xs = [np.zeros_like(b) for b in bs]
     s.solve([Field(x, lo_of(L)) for x, L in zip(xs, Ls)], [Field(b, lo_of(L)) for b, L in zip(bs, Ls)], tol, 0.0)
     return xs, s.stats
-
-
-def polycrystal_amr(n=16, nlev=2, seed=1):
-    Ls = po.amr_levels(n, nlev)
-    bc = bc_config0()
-    seeds = microstructure.voronoi_seeds(8, seed)
-    rot = models.random_rotations(8, np.random.default_rng(seed + 1))
-    tab = models.cubic(1.68, 1.21, 0.75, rot)
-    Cs, bs = [], []
-    for L in Ls:
-        lo = [L.lo[d] - L.ng for d in range(3)]
-        hi = [L.hi[d] + L.ng for d in range(3)]
-        gid = microstructure.voronoi_grain_ids(lo, hi, tuple(L.dx), seeds)
-        Cs.append(np.ascontiguousarray(np.moveaxis(tab[gid], -1, 0)))
-        bs.append(po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)))
-    return Ls, Cs, bc, bs
 
 
 @pytest.mark.parametrize("nlev", [2, 3])
