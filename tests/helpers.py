@@ -95,3 +95,20 @@ def polycrystal_amr(n=16, nlev=2, seed=1):
         Cs.append(np.ascontiguousarray(np.moveaxis(tab[gid], -1, 0)))
         bs.append(po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)))
     return Ls, Cs, bc, bs
+
+
+def golden_stiffness(parts):
+    """The per-node stiffness of a golden case: stored whole, or as table[gid] * scale."""
+    if "C" in parts:
+        return np.ascontiguousarray(parts["C"])
+    C = np.moveaxis(parts["tabs"][parts["gid"].astype(np.intp)], -1, 0) * parts["scale"][None]
+    return np.ascontiguousarray(C)
+
+
+def golden_case(z, name):
+    """Case `name` ("iso", "mm", "diag" or "solve") of tests/golden/elastic_ops.npz as a dict
+    with the keys the generator wrote, minus the prefix, plus the rebuilt stiffness "C"."""
+    p = name + "_"
+    d = {k[len(p):]: z[k] for k in z.files if k.startswith(p)}
+    d["C"] = golden_stiffness(d)
+    return d
