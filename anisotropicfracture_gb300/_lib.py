@@ -84,6 +84,8 @@ SIGNATURES = {
     "ae_op_set_model": ([P, C.c_int, FAB], C.c_int),
     "ae_op_set_model_uniform": ([P, C.POINTER(C.c_double), C.c_int], C.c_int),
     "ae_op_set_model_grains": ([P, C.c_int, FAB, C.c_int, C.c_void_p], C.c_int),
+    "ae_op_set_model_mixture": ([P, C.c_int, FAB, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ae_op_set_model_degraded": ([P, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double], C.c_int),
     "ae_op_set_bc": ([P, C.POINTER(C.c_int), C.POINTER(C.c_double)], C.c_int),
     "ae_op_set_flags": ([P, C.c_int, C.c_int], C.c_int),
     "ae_op_prepare": ([P], C.c_int),

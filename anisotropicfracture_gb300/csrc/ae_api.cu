@@ -140,6 +140,8 @@ struct ae_op_s {
     size_t stage_bytes = 0;
     void* stage2 = nullptr;
     size_t stage2_bytes = 0;
+    void* mixtab = nullptr;  // device copy of the per-phase tables of ae_op_set_model_mixture
+    size_t mixtab_bytes = 0;
 
     template <class T>
     T* alloc(long long n) {
@@ -154,6 +156,7 @@ struct ae_op_s {
         for (void* p : allocs) cudaFree(p);
         if (stage) cudaFree(stage);
         if (stage2) cudaFree(stage2);
+        if (mixtab) cudaFree(mixtab);
         if (hnorm) cudaFreeHost(hnorm);
         if (own_st) cudaStreamDestroy(own_st);
         if (ev_in) cudaEventDestroy(ev_in);
@@ -1002,6 +1005,96 @@ int ae_op_set_model_grains(ae_op* op, int amrlev, const ae_fab* grain_id, int ng
         require(bad == 0, "SetModelGrains: a grain id is outside [0, ngrains)");
         L.ngrains = ngrains;
         L.grains = true;
+        op->amr[amrlev].model_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_model_mixture(ae_op* op, int amrlev, const ae_fab* eta, int nphase, const double* table,
+                            const double* F0table, const ae_fab* F0) {
+    return guarded([&] {
+        require(op != nullptr && table != nullptr, "null argument");
+        require(nphase >= 1, "SetModelMixture: at least one phase");
+        require((F0table == nullptr) == (F0 == nullptr), "SetModelMixture: F0table and F0 go together");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 need = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        // node (i, j, k) reads cells (i-1..i, j-1..j, k)
+        Box3 cells = need;
+        cells.lo[0] -= 1;
+        cells.lo[1] -= 1;
+        check_fab(eta, cells, nphase, "SetModelMixture eta");
+        require(!eta->is_float, "SetModelMixture: eta must be double");
+        View<double> f0v{};
+        if (F0) {
+            check_fab(F0, need, 9, "SetModelMixture F0");
+            require(!F0->is_float, "SetModelMixture: F0 must be double");
+        }
+        const int nc = op->ncoef;
+        const size_t tab_n = (size_t)nphase * nc, f0_n = F0table ? (size_t)nphase * 9 : 0;
+        ensure_stage(op->mixtab, op->mixtab_bytes, sizeof(double) * (tab_n + f0_n));
+        double* dtab = static_cast<double*>(op->mixtab);
+        AE_CHECK(cudaMemcpyAsync(dtab, table, sizeof(double) * tab_n, cudaMemcpyDefault, op->st));
+        if (F0table)
+            AE_CHECK(cudaMemcpyAsync(dtab + tab_n, F0table, sizeof(double) * f0_n, cudaMemcpyDefault, op->st));
+        View<const double> ev = device_view_in(op, *eta, 0);
+        const bool f0_host = F0 && !is_device_ptr(F0->data);
+        if (F0) {
+            if (f0_host) {
+                // stage the whole host fab so that the nodes outside the region come back unchanged
+                const size_t bytes = sizeof(double) * (size_t)fab_elems(*F0);
+                ensure_stage(op->stage2, op->stage2_bytes, bytes);
+                AE_CHECK(cudaMemcpyAsync(op->stage2, F0->data, bytes, cudaMemcpyHostToDevice, op->st));
+                ae_fab d = *F0;
+                d.data = op->stage2;
+                f0v = fab_view<double>(d);
+            } else {
+                f0v = fab_view<double>(*F0);
+            }
+        }
+        op->amr[amrlev].model_set = false;
+        AE_CHECK(cudaMemsetAsync(op->dflag, 0, sizeof(int), op->st));
+        launch_model_mixture(need, nc, ev, nphase, dtab, F0table ? dtab + tab_n : nullptr, level_view(L.g, L.C), f0v,
+                             op->dflag, op->st);
+        int bad = 0;
+        AE_CHECK(cudaMemcpyAsync(&bad, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, op->st));
+        if (f0_host)
+            AE_CHECK(cudaMemcpyAsync(F0->data, op->stage2, sizeof(double) * (size_t)fab_elems(*F0),
+                                     cudaMemcpyDeviceToHost, op->st));
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        require(bad == 0, "SetModelMixture: the order parameters sum to zero at a node");
+        L.grains = false;
+        op->amr[amrlev].model_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_op_set_model_degraded(ae_op* op, int amrlev, const ae_fab* eta, int neta, double lambda0, double mu0) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(op->ncoef == 2, "SetModelDegraded: isotropic operators only");
+        require(neta >= 0, "SetModelDegraded: negative component count");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 need = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        const Box3 valid = box_isect(geo_valid(L.g), geo_domain(L.g));
+        View<const double> ev{};
+        if (neta > 0) {
+            // node (i, j, k) reads cells (i-1..i, j-1..j, k-1..k)
+            Box3 cells = valid;
+            for (int d = 0; d < 3; ++d) cells.lo[d] -= 1;
+            check_fab(eta, cells, neta, "SetModelDegraded eta");
+            require(!eta->is_float, "SetModelDegraded: eta must be double");
+            ev = device_view_in(op, *eta, 0);
+        }
+        op->amr[amrlev].model_set = false;
+        AE_CHECK(cudaMemsetAsync(op->dflag, 0, sizeof(int), op->st));
+        launch_model_degraded(need, valid, ev, neta, lambda0, mu0, level_view(L.g, L.C), op->dflag, op->st);
+        int bad = 0;
+        AE_CHECK(cudaMemcpyAsync(&bad, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, op->st));
+        AE_CHECK(cudaStreamSynchronize(op->st));
+        require(bad == 0, "SetModelDegraded: an order parameter's cell mean is outside [0, 1]");
+        L.grains = false;
         op->amr[amrlev].model_set = true;
         op->prepared = false;
     });

@@ -78,6 +78,104 @@ void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned sh
     launched();
 }
 
+// ------------------------------------------------------------------ stiffness from order parameters
+// Phase-field mixture, src/Integrator/PhaseFieldMicrostructure.cpp:531-539 with
+// Affine::Cubic::Combine (src/Model/Solid/Affine/Cubic.H:70-82): the weight of phase n at a node
+// is its mean over the four cells (i-1..i, j-1..j) of cell layer k, divided by the sum of those
+// means; stiffness slots and eigenstrain are the weighted sums of the per-phase tables.
+template <int NC>
+__global__ void __launch_bounds__(kBlock) k_model_mixture(Reg reg, View<const double> eta, int np,
+                                                          const double* __restrict__ tab,
+                                                          const double* __restrict__ f0tab, View<double> C,
+                                                          View<double> F0, int* bad) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long o00 = eta.at(i, j, k), o01 = eta.at(i, j - 1, k);
+    const long long o10 = eta.at(i - 1, j, k), o11 = eta.at(i - 1, j - 1, k);
+    double sum = 0.0;
+    for (int n = 0; n < np; ++n) {
+        const double* e = eta.p + n * eta.sc;
+        sum += 0.25 * (e[o00] + e[o01] + e[o10] + e[o11]);
+    }
+    if (sum == 0.0 || isnan(sum)) {
+        atomicExch(bad, 1);
+        return;
+    }
+    double acc[NC], f[9];
+    for (int q = 0; q < NC; ++q) acc[q] = 0.0;
+    for (int r = 0; r < 9; ++r) f[r] = 0.0;
+    for (int n = 0; n < np; ++n) {
+        const double* e = eta.p + n * eta.sc;
+        const double w = 0.25 * (e[o00] + e[o01] + e[o10] + e[o11]) / sum;
+        for (int q = 0; q < NC; ++q) acc[q] += tab[n * NC + q] * w;
+        if (F0.p)
+            for (int r = 0; r < 9; ++r) f[r] += f0tab[n * 9 + r] * w;
+    }
+    const long long o = C.at(i, j, k);
+    for (int q = 0; q < NC; ++q) C.p[o + q * C.sc] = acc[q];
+    if (F0.p) {
+        const long long of = F0.at(i, j, k);
+        for (int r = 0; r < 9; ++r) F0.p[of + r * F0.sc] = f[r];
+    }
+}
+void launch_model_mixture(const Box3& region, int nc, View<const double> eta, int np, const double* tab,
+                          const double* f0tab, View<double> C, View<double> F0, int* bad, cudaStream_t st) {
+    const Reg reg = make_reg(region);
+    if (reg.n == 0) return;
+    if (nc == 2)
+        k_model_mixture<2><<<nblocks(reg.n), kBlock, 0, st>>>(reg, eta, np, tab, f0tab, C, F0, bad);
+    else if (nc == 9)
+        k_model_mixture<9><<<nblocks(reg.n), kBlock, 0, st>>>(reg, eta, np, tab, f0tab, C, F0, bad);
+    else
+        k_model_mixture<21><<<nblocks(reg.n), kBlock, 0, st>>>(reg, eta, np, tab, f0tab, C, F0, bad);
+    launched();
+}
+
+// Isotropic degradation, src/Integrator/PolymerDegradation.cpp:794-833 with
+// Degradable::Isotropic::DegradeModulus (src/Model/Solid/LinearElastic/Degradable/Isotropic.H:74-81):
+// every node starts undamaged; each valid node takes (lambda0 (1 - e), mu0 (1 - e)) with e the
+// mean of an order parameter over the 8 cells around the node.  Each component is averaged and
+// range-checked in turn and the last one is kept, as the reference's loop over components does.
+__global__ void __launch_bounds__(kBlock) k_model_degraded(Reg reg, Box3 valid, View<const double> eta, int neta,
+                                                           double lam0, double mu0, View<double> C, int* bad) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double lam = lam0, mu = mu0;
+    const bool in_valid = i >= valid.lo[0] && i <= valid.hi[0] && j >= valid.lo[1] && j <= valid.hi[1] &&
+                          k >= valid.lo[2] && k <= valid.hi[2];
+    if (in_valid && neta > 0) {
+        const long long c000 = eta.at(i, j, k), c100 = eta.at(i - 1, j, k);
+        const long long c010 = eta.at(i, j - 1, k), c110 = eta.at(i - 1, j - 1, k);
+        const long long c001 = eta.at(i, j, k - 1), c101 = eta.at(i - 1, j, k - 1);
+        const long long c011 = eta.at(i, j - 1, k - 1), c111 = eta.at(i - 1, j - 1, k - 1);
+        double e = 0.0;
+        for (int n = 0; n < neta; ++n) {
+            const double* p = eta.p + n * eta.sc;
+            e = 0.125 * (p[c000] + p[c100] + p[c010] + p[c110] + p[c001] + p[c101] + p[c011] + p[c111]);
+            if (!(e >= 0.0 && e <= 1.0)) {
+                atomicExch(bad, 1);
+                return;
+            }
+        }
+        lam = lam0 * (1.0 - e);
+        mu = mu0 * (1.0 - e);
+    }
+    const long long o = C.at(i, j, k);
+    C.p[o] = lam;
+    C.p[o + C.sc] = mu;
+}
+void launch_model_degraded(const Box3& region, const Box3& valid, View<const double> eta, int neta, double lam0,
+                           double mu0, View<double> C, int* bad, cudaStream_t st) {
+    const Reg reg = make_reg(region);
+    if (reg.n == 0) return;
+    k_model_degraded<<<nblocks(reg.n), kBlock, 0, st>>>(reg, valid, eta, neta, lam0, mu0, C, bad);
+    launched();
+}
+
 // ------------------------------------------------------------------ Strain / Stress / Energy
 // src/Operator/Elastic.cpp:399-572 (valid box, boundary-aware first derivatives)
 __device__ __forceinline__ void grad_at(const Geo& g, const SCoef<double>& K, const View<const double>& u, int i,

@@ -162,6 +162,14 @@ void launch_newton_post(const OpParams& P, View<const double> C, View<const doub
 // stiffness C = tab[id]; tab32 = (float) tab.  *bad is set if an id is outside [0, ng).
 void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned short> gid, View<double> C,
                        const double* tab, int ng, int nc, float* tab32, int* bad, cudaStream_t st);
+// Phase-field mixture over `region` (nodes): eta is cell-centred with np components, tab np x nc,
+// f0tab np x 9 (read only when F0.p is set).  *bad is set where the order parameters sum to zero.
+void launch_model_mixture(const Box3& region, int nc, View<const double> eta, int np, const double* tab,
+                          const double* f0tab, View<double> C, View<double> F0, int* bad, cudaStream_t st);
+// Degraded isotropic stiffness over `region` (nodes); only nodes in `valid` read eta (cell-centred,
+// neta components).  *bad is set where a cell mean lies outside [0, 1].
+void launch_model_degraded(const Box3& region, const Box3& valid, View<const double> eta, int neta, double lam0,
+                           double mu0, View<double> C, int* bad, cudaStream_t st);
 
 struct BottomArgs {
     OpParams P;

@@ -175,6 +175,35 @@ class Elastic:
         f.is_float = 0
         check(load().ae_op_set_model_grains(self._h, int(a), C.byref(f), table.shape[0], table.ctypes.data))
 
+    def SetModelMixture(self, a, eta, table, F0table=None, F0=None):
+        """SetModel(amrlev, ...) from cell-centred phase-field order parameters, mixed on the
+        device as PhaseFieldMicrostructure::TimeStepBegin does with Affine::Cubic::Combine
+        (src/Integrator/PhaseFieldMicrostructure.cpp:516-541, src/Model/Solid/Affine/Cubic.H:70-82).
+        eta: a Field of FP64 cell values (nphase components) whose box is in cell indices;
+        table (nphase, ncoef).  F0table (nphase, 9) and F0 (a 9-component nodal Field) go
+        together: F0 receives the mixed eigenstrain."""
+        if (F0table is None) != (F0 is None):
+            raise ValueError("F0table and F0 go together")
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        fe = eta.fab()
+        f0t = None if F0table is None else np.ascontiguousarray(F0table, dtype=np.float64)
+        ff = None if F0 is None else F0.fab()
+        check(load().ae_op_set_model_mixture(self._h, int(a), C.byref(fe), table.shape[0], table.ctypes.data,
+                                             None if f0t is None else f0t.ctypes.data,
+                                             None if ff is None else C.addressof(ff)))
+
+    def SetModelDegraded(self, a, eta, lambda0, mu0):
+        """SetModel(amrlev, ...) for the isotropic degradable model, built on the device as
+        PolymerDegradation::DegradeMaterial does (src/Integrator/PolymerDegradation.cpp:794-833):
+        (lambda0, mu0) everywhere, (1 - e) times that on valid nodes, e the 8-cell mean of eta
+        (a Field of FP64 cell values, box in cell indices; None for no degradation)."""
+        if eta is None:
+            check(load().ae_op_set_model_degraded(self._h, int(a), None, 0, float(lambda0), float(mu0)))
+            return
+        fe = eta.fab()
+        check(load().ae_op_set_model_degraded(self._h, int(a), C.addressof(fe), fe.ncomp, float(lambda0),
+                                              float(mu0)))
+
     def SetBC(self, bc):
         self.m_bc = bc
         t = np.ascontiguousarray(bc.type, dtype=np.int32)

@@ -133,6 +133,34 @@ int ae_op_set_model_uniform(ae_op* op, const double* coeffs, int ncoef);
  * the level then read 2-byte grain ids and the table instead of 84/168 bytes per node, with the
  * same arithmetic on the same values. */
 int ae_op_set_model_grains(ae_op* op, int amrlev, const ae_fab* grain_id, int ngrains, const double* table);
+/* SetModel from cell-centred phase-field order parameters, built on the device.  Replaces the
+ * model field PhaseFieldMicrostructure::TimeStepBegin fills before its elastic solve
+ * (src/Integrator/PhaseFieldMicrostructure.cpp:516-541), node by node, with
+ * Affine::Cubic::Combine (src/Model/Solid/Affine/Cubic.H:70-82).
+ *  - eta: nphase components, FP64, cell-centred (cell (i,j,k) spans nodes i..i+1, ...), covering
+ *    cells [lo-1, hi] in x and y and [lo, hi] in z of the SetModel region (ae_op_set_model).
+ *  - At node (i,j,k): e_n = (eta_n(i,j,k) + eta_n(i,j-1,k) + eta_n(i-1,j,k) + eta_n(i-1,j-1,k)) / 4
+ *    (the reference averages over the four cells of the x-y plane at cell layer k, in 3-D too)
+ *    and C = sum_n table[n] e_n / sum_m e_m.  table: nphase x ncoef.
+ *  - F0table (nphase x 9, row-major) and F0 (9 components over the SetModel region) are optional
+ *    together: F0 receives the eigenstrain mixed with the same weights, as ae_newton_residual and
+ *    ae_newton_dw take it.
+ *  - Host or device memory.  AE_ERR_ARG where the order parameters sum to zero at a node (the
+ *    reference divides by zero there). */
+int ae_op_set_model_mixture(ae_op* op, int amrlev, const ae_fab* eta, int nphase, const double* table,
+                            const double* F0table, const ae_fab* F0);
+/* SetModel for the isotropic degradable model, built on the device: PolymerDegradation::
+ * DegradeMaterial (src/Integrator/PolymerDegradation.cpp:794-833) with
+ * Degradable::Isotropic::DegradeModulus (src/Model/Solid/LinearElastic/Degradable/Isotropic.H:74-81).
+ *  - Every node of the SetModel region gets (lambda0, mu0).  Each valid node then gets
+ *    (lambda0 (1 - e), mu0 (1 - e)), e the mean of eta over the 8 cells around the node.  With
+ *    several components each is averaged and range-checked in turn and the last one is kept, as
+ *    the reference's loop does.
+ *  - eta: neta components, FP64, cell-centred, covering cells [lo-1, hi] of the valid box; host
+ *    or device memory; may be NULL when neta = 0.
+ *  - Isotropic operators only.  AE_ERR_ARG where a mean lies outside [0, 1] (the reference
+ *    aborts) or is NaN. */
+int ae_op_set_model_degraded(ae_op* op, int amrlev, const ae_fab* eta, int neta, double lambda0, double mu0);
 /* BC::Operator::Elastic<T>::Set for all 26 faces (Elastic.H:61-69); val used by ae_bc_init. */
 int ae_op_set_bc(ae_op* op, const int* type /*[26][3]*/, const double* val /*[26][3]*/);
 /* Operator::Elastic<T>::SetUniform / SetHomogeneous (Elastic.H:48,111). */

@@ -221,6 +221,30 @@ public:
         const ae_fab f = coeffs.c();
         alamo::check(ae_op_set_model(m_op, amrlev, &f));
     }
+    // The model field PhaseFieldMicrostructure::TimeStepBegin mixes from its order parameters
+    // (PhaseFieldMicrostructure.cpp:516-541, Affine::Cubic::Combine), built on the device: eta is
+    // the cell-centred order-parameter fab, one model per phase; F0 (9 components) receives the
+    // mixed eigenstrain when the phases carry one (F0tab: nphase x 9, row-major).
+    void SetModelMixture(int amrlev, const alamo::Fab& eta, const std::vector<T>& phases,
+                         const std::vector<double>* F0tab = nullptr, alamo::Fab* F0 = nullptr) {
+        std::vector<double> tab(phases.size() * T::ncoef);
+        for (size_t n = 0; n < phases.size(); ++n) {
+            double c[21];
+            phases[n].coeffs(c);
+            for (int q = 0; q < T::ncoef; ++q) tab[n * T::ncoef + q] = c[q];
+        }
+        const ae_fab fe = eta.c();
+        ae_fab ff{};
+        if (F0) ff = F0->c();
+        alamo::check(ae_op_set_model_mixture(m_op, amrlev, &fe, (int)phases.size(), tab.data(),
+                                             F0tab ? F0tab->data() : nullptr, F0 ? &ff : nullptr));
+    }
+    // PolymerDegradation::DegradeMaterial (PolymerDegradation.cpp:794-833) for the isotropic
+    // degradable model, built on the device from the cell-centred damage fab eta.
+    void SetModelDegraded(int amrlev, const alamo::Fab& eta, double lambda0, double mu0) {
+        const ae_fab fe = eta.c();
+        alamo::check(ae_op_set_model_degraded(m_op, amrlev, &fe, fe.ncomp, lambda0, mu0));
+    }
     // SetBC stores the table; the reference keeps a non-owning pointer (Elastic.H:58-66)
     void SetBC(BC::Operator::Elastic<T>* bc) {
         m_bc = bc;

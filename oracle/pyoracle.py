@@ -294,6 +294,68 @@ def newton_dw(L, model, Cf, u, F0=None):
     return dw, w
 
 
+# ---------------------------------------------------------------- stiffness from order parameters
+def _cells(eta, eta_lo, lo, hi, di, dj, dk):
+    """eta over the nodal box [lo, hi] shifted by (di, dj, dk) cells: the array of
+    eta(i + di, j + dj, k + dk) for every node (i, j, k) of the box, all components."""
+    sl = tuple(slice(lo[d] + s - eta_lo[d], hi[d] + s - eta_lo[d] + 1) for d, s in ((2, dk), (1, dj), (0, di)))
+    for a, q in enumerate(sl):
+        if q.start < 0 or q.stop > eta.shape[1 + a]:
+            raise IndexError("eta does not cover the cells the nodes read")
+    return eta[(slice(None),) + sl]
+
+
+def model_mixture(lo, hi, eta, eta_lo, table, F0table=None):
+    """The phase-field model field restated (src/Integrator/PhaseFieldMicrostructure.cpp:531-539
+    with Affine::Cubic::Combine, src/Model/Solid/Affine/Cubic.H:70-82) over the nodal box
+    [lo, hi]: e_n = 0.25 (eta_n(i,j,k) + eta_n(i,j-1,k) + eta_n(i-1,j,k) + eta_n(i-1,j-1,k)),
+    C = sum_n table[n] (e_n / sum_m e_m), summed from zero in phase order, and F0 likewise.
+    eta: (nphase, cz, cy, cx) cell values whose first cell is eta_lo.  Where the e_n sum to zero
+    the reference divides by zero, and so does this (NaN)."""
+    table = np.asarray(table, dtype=np.float64)
+    e = 0.25 * (_cells(eta, eta_lo, lo, hi, 0, 0, 0) + _cells(eta, eta_lo, lo, hi, 0, -1, 0)
+                + _cells(eta, eta_lo, lo, hi, -1, 0, 0) + _cells(eta, eta_lo, lo, hi, -1, -1, 0))
+    s = np.zeros(e.shape[1:])
+    for n in range(e.shape[0]):
+        s = s + e[n]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        w = e / s[None]
+    Cm = np.zeros((table.shape[1],) + e.shape[1:])
+    for n in range(e.shape[0]):
+        Cm = Cm + table[n][:, None, None, None] * w[n][None]
+    F0 = None
+    if F0table is not None:
+        F0table = np.asarray(F0table, dtype=np.float64)
+        F0 = np.zeros((9,) + e.shape[1:])
+        for n in range(e.shape[0]):
+            F0 = F0 + F0table[n][:, None, None, None] * w[n][None]
+    return Cm, F0
+
+
+def model_degraded(lo, hi, vlo, vhi, eta, eta_lo, lambda0, mu0):
+    """The degradable isotropic model field restated (src/Integrator/PolymerDegradation.cpp:794-833,
+    src/Model/Solid/LinearElastic/Degradable/Isotropic.H:74-81) over the nodal box [lo, hi]:
+    (lambda0, mu0) everywhere; on the valid nodes [vlo, vhi], for each component in turn,
+    e = (1/8) times the sum of its 8 cells around the node (the reference's order) checked to lie
+    in [0, 1] (ValueError otherwise, where the reference aborts), the last one kept:
+    (lambda0 (1 - e), mu0 (1 - e))."""
+    shape = tuple(hi[d] - lo[d] + 1 for d in (2, 1, 0))
+    Cm = np.empty((2,) + shape)
+    Cm[0], Cm[1] = lambda0, mu0
+    if eta is None or eta.shape[0] == 0:
+        return Cm
+    c = lambda di, dj, dk: _cells(eta, eta_lo, vlo, vhi, di, dj, dk)
+    e = 0.125 * (c(0, 0, 0) + c(-1, 0, 0) + c(0, -1, 0) + c(-1, -1, 0)
+                 + c(0, 0, -1) + c(-1, 0, -1) + c(0, -1, -1) + c(-1, -1, -1))
+    for n in range(e.shape[0]):
+        if not np.all((e[n] >= 0.0) & (e[n] <= 1.0)):
+            raise ValueError("Invalid value of eta")
+    v = tuple(slice(vlo[d] - lo[d], vhi[d] - lo[d] + 1) for d in (2, 1, 0))
+    Cm[(0,) + v] = lambda0 * (1.0 - e[-1])
+    Cm[(1,) + v] = mu0 * (1.0 - e[-1])
+    return Cm
+
+
 # ---------------------------------------------------------------- periodic cells
 class RveLevel(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("pad_", C.c_int), ("dx", C.c_double * 3)]
