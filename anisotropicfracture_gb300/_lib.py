@@ -135,6 +135,8 @@ SIGNATURES = {
     "ae_server_wait": ([P, C.c_longlong, C.c_double, C.POINTER(RequestInfo), C.POINTER(CellStats), DP], C.c_int),
     "ae_server_release": ([P, C.c_longlong], C.c_int),
     "ae_server_get_stats": ([P, C.POINTER(ServerStats)], C.c_int),
+    "ae_write_plotfile": ([C.c_char_p, C.c_int, C.POINTER(LevelDesc), FAB, C.c_int, C.POINTER(C.c_char_p),
+                           C.c_double, C.POINTER(C.c_int)], C.c_int),
 }
 
 _lib = None

@@ -17,7 +17,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxe
          "-I", CSRC, "-I", INCLUDE]
 
 SOURCES = ["ae_kernels_f64.cu", "ae_kernels_f32.cu", "ae_api.cu", "ae_noalloc.cu", "ae_cells_kernels.cu",
-           "ae_cells.cu", "ae_server.cu"]
+           "ae_cells.cu", "ae_server.cu", "ae_plotfile.cpp"]
 
 
 def _deps():
@@ -32,7 +32,7 @@ EXTRA = os.environ.get("AE_NVCC_FLAGS", "").split()
 
 
 def _compile(src):
-    obj = os.path.join(OBJ, src.replace(".cu", ".o"))
+    obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     cmd = [NVCC] + ARCH + FLAGS + EXTRA + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -215,6 +215,16 @@ int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fa
 int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
              const ae_solver_opts* opts, ae_solve_stats* stats);
 
+/* The nodal plotfile of Integrator::WritePlotFile (src/Integrator/Integrator.cpp:582-681, the
+ * "node" half, written by amrex::WriteMultiLevelPlotfile): an AMReX plotfile directory
+ * (HyperCLaw-V1.1 Header; Level_<l>/Cell_H and Cell_D_00000) holding ncomp nodal components on
+ * each level's valid box, one patch per level.  fabs: one FP64 HOST fab per level covering its
+ * valid box (ghost nodes are not written); names: ncomp component names without whitespace (the
+ * reference names a vector field's components name001, name002, ...); steps: per-level step
+ * numbers or NULL.  AE_ERR_NAN if a written value is NaN or infinite. */
+int ae_write_plotfile(const char* dir, int nlevels, const ae_level_desc* levels, const ae_fab* fabs, int ncomp,
+                      const char* const* names, double time, const int* steps);
+
 /* Device memory of the operator (bytes), for admission control. */
 long long ae_op_device_bytes(const ae_op* op);
 
