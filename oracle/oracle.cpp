@@ -1629,29 +1629,11 @@ inline void newton_dw_node(const Lev& L, int model, const double* C, const doubl
     stress_of(model, a, e, sig);
 }
 
-}  // namespace
-
-extern "C" {
-
-// Newton::prepareForSolve (src/Solver/Nonlocal/Newton.H:30-139) on one box: dw = DW(grad u) on
-// grow(valid, 2) ∩ domain, stencils one-sided at that box's faces; then on grow(valid, 1) ∩ domain
-// rhs = b - BC(u, grad u, dw) on the domain boundary (BC faces classified against that box) and
-// rhs = b - div(dw) by central differences inside.  Nodes outside keep rhs.
-int orc_newton_residual(const orc_level* L0, int model, const double* C, const int* bctype, const double* u,
-                        const double* b, const double* F0, double* rhs) {
-    const Lev L(*L0);
-    const Box bx2 = isect(isect(grow(L.valid, 2), L.dom), L.store);
-    std::vector<double> dw(9 * L.nn, 0.0);
-    for_box(bx2, [&](int i, int j, int k) {
-        int st[3];
-        box_stencil(bx2, i, j, k, st);
-        const long c = L.at(i, j, k);
-        double g[3][3], s[3][3];
-        newton_grad(L, u, st, c, g);
-        newton_dw_node(L, model, C, F0, g, c, s);
-        for (int p = 0; p < 3; ++p)
-            for (int d = 0; d < 3; ++d) dw[(3 * p + d) * L.nn + c] = s[p][d];
-    });
+// Second half of Newton::prepareForSolve (src/Solver/Nonlocal/Newton.H:84-136): on
+// grow(valid, 1) ∩ domain, rhs = b - BC(u, grad u, dw) on the domain boundary (BC faces
+// classified against that box) and rhs = b - div(dw) by central differences inside.
+void newton_rhs_from_dw(const Lev& L, const int* bctype, const double* u, const double* b, const double* dw,
+                        double* rhs) {
     const Box bx1 = isect(isect(grow(L.valid, 1), L.dom), L.store);
     for_box(bx1, [&](int i, int j, int k) {
         const long c = L.at(i, j, k);
@@ -1681,6 +1663,59 @@ int orc_newton_residual(const orc_level* L0, int model, const double* C, const i
             }
         }
     });
+}
+
+}  // namespace
+
+extern "C" {
+
+// Newton::prepareForSolve (src/Solver/Nonlocal/Newton.H:30-139) on one box: dw = DW(grad u) on
+// grow(valid, 2) ∩ domain, stencils one-sided at that box's faces; then rhs from dw as in
+// newton_rhs_from_dw.  Nodes outside grow(valid, 1) ∩ domain keep rhs.
+int orc_newton_residual(const orc_level* L0, int model, const double* C, const int* bctype, const double* u,
+                        const double* b, const double* F0, double* rhs) {
+    const Lev L(*L0);
+    const Box bx2 = isect(isect(grow(L.valid, 2), L.dom), L.store);
+    std::vector<double> dw(9 * L.nn, 0.0);
+    for_box(bx2, [&](int i, int j, int k) {
+        int st[3];
+        box_stencil(bx2, i, j, k, st);
+        const long c = L.at(i, j, k);
+        double g[3][3], s[3][3];
+        newton_grad(L, u, st, c, g);
+        newton_dw_node(L, model, C, F0, g, c, s);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) dw[(3 * p + d) * L.nn + c] = s[p][d];
+    });
+    newton_rhs_from_dw(L, bctype, u, b, dw.data(), rhs);
+    return 0;
+}
+
+// The kinematic input of Newton::prepareForSolve for any model: grad u on grow(valid, 2) ∩ domain
+// with the stencils one-sided at that box's faces (Newton.H:52-58), 9 components row-major
+// (gradu(3 p + d) = du_p / dx_d).  Other nodes are not written.
+int orc_newton_grad(const orc_level* L0, const double* u, double* gradu) {
+    const Lev L(*L0);
+    const Box bx2 = isect(isect(grow(L.valid, 2), L.dom), L.store);
+    for_box(bx2, [&](int i, int j, int k) {
+        int st[3];
+        box_stencil(bx2, i, j, k, st);
+        const long c = L.at(i, j, k);
+        double g[3][3];
+        newton_grad(L, u, st, c, g);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) gradu[(3 * p + d) * L.nn + c] = g[p][d];
+    });
+    return 0;
+}
+
+// rhs = b - N(u) for a model whose DW the caller evaluated (e.g. a finite-kinematics model at
+// F = I + grad u, Newton.H:70-75): dw holds 9 components over the storage box, set on
+// grow(valid, 2) ∩ domain.
+int orc_newton_residual_dw(const orc_level* L0, const int* bctype, const double* u, const double* b,
+                           const double* dw, double* rhs) {
+    const Lev L(*L0);
+    newton_rhs_from_dw(L, bctype, u, b, dw, rhs);
     return 0;
 }
 

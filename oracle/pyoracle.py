@@ -294,6 +294,83 @@ def newton_dw(L, model, Cf, u, F0=None):
     return dw, w
 
 
+def newton_grad(L, u):
+    """grad u (9 components, row-major) on grow(valid, 2) ∩ domain with Newton::prepareForSolve's
+    stencils (src/Solver/Nonlocal/Newton.H:52-58); zero elsewhere."""
+    lb = lib()
+    d = C.POINTER(C.c_double)
+    lb.orc_newton_grad.argtypes = [C.POINTER(Level), d, d]
+    g = np.zeros((9,) + L.shape)
+    u = _f64(u)
+    lb.orc_newton_grad(C.byref(L), _d(u), _d(g))
+    return g
+
+
+def newton_residual_dw(L, bctype, u, b, dw, rhs=None):
+    """rhs = b - N(u) from a DW field the caller evaluated (9 components over the storage box),
+    as Newton::prepareForSolve forms it (src/Solver/Nonlocal/Newton.H:84-136)."""
+    lb = lib()
+    d = C.POINTER(C.c_double)
+    lb.orc_newton_residual_dw.argtypes = [C.POINTER(Level), C.POINTER(C.c_int), d, d, d, d]
+    out = np.array(b if rhs is None else rhs, dtype=np.float64, copy=True)
+    u, b, dw = _f64(u), _f64(b), _f64(dw)
+    bt, bp = _i(bctype)
+    lb.orc_newton_residual_dw(C.byref(L), bp, _d(u), _d(b), _d(dw), _d(out))
+    return out
+
+
+def neohookean_newton_residual(L, mu, kappa, bctype, u, b):
+    """Newton::prepareForSolve for Model::Solid::Elastic::NeoHookean (kinematic variable F,
+    Newton.H:70-75): dw = DW(I + grad u) node by node, then rhs = b - N(u).  Also returns the
+    tangent DDW(I + grad u) per node, shaped (nz, ny, nx, 3, 3, 3, 3)."""
+    g = newton_grad(L, u)
+    F = np.moveaxis(g, 0, -1).reshape(L.shape + (3, 3)) + np.eye(3)
+    dw = np.ascontiguousarray(np.moveaxis(neohookean_dw(F, mu, kappa).reshape(L.shape + (9,)), -1, 0))
+    return newton_residual_dw(L, bctype, u, b, dw), neohookean_ddw(F, mu, kappa)
+
+
+# ---------------------------------------------------------------- NeoHookean (finite kinematics)
+def _neo_parts(F):
+    F = np.asarray(F, dtype=np.float64)
+    J = np.linalg.det(F)
+    J23 = np.abs(J) ** (2.0 / 3.0)
+    tr = np.einsum("...ij,...ij->...", F, F)  # trace(F F^T)
+    FinvT = np.swapaxes(np.linalg.inv(F), -1, -2)
+    return F, J, J23, tr, FinvT
+
+
+def neohookean_w(F, mu, kappa):
+    """Model::Solid::Elastic::NeoHookean::W (src/Model/Solid/Elastic/NeoHookean.H:19-27):
+    mu/2 (tr(F F^T) / |J|^(2/3) - 3) + kappa/2 (J - 1)^2.  F: (..., 3, 3)."""
+    F, J, J23, tr, _ = _neo_parts(F)
+    return 0.5 * mu * (tr / J23 - 3.0) + 0.5 * kappa * (J - 1.0) * (J - 1.0)
+
+
+def neohookean_dw(F, mu, kappa):
+    """NeoHookean::DW (NeoHookean.H:28-39): mu (F / J23 - tr F^-T / (3 J23)) + kappa (J - 1) J F^-T."""
+    F, J, J23, tr, FinvT = _neo_parts(F)
+    J23, tr, J = J23[..., None, None], tr[..., None, None], J[..., None, None]
+    return mu * (F / J23 - tr * FinvT / (3.0 * J23)) + kappa * (J - 1.0) * J * FinvT
+
+
+def neohookean_ddw(F, mu, kappa):
+    """NeoHookean::DDW (NeoHookean.H:40-66), the Sym::Major tangent ddw[..., i, j, k, l]:
+    (mu / J23) t1 + kappa J t2 with
+    t1 = d_ik d_jl - 2/3 F_ij G_kl - 2/3 G_ij F_kl + 2/9 tr G_ij G_kl + 1/3 tr G_il G_kj,
+    t2 = (2J - 1) G_ij G_kl + (1 - J) G_il G_kj,  G = F^-T."""
+    F, J, J23, tr, G = _neo_parts(F)
+    I = np.eye(3)
+    d = np.einsum("ik,jl->ijkl", I, I)
+    t1 = (d - (2.0 / 3.0) * np.einsum("...ij,...kl->...ijkl", F, G)
+          - (2.0 / 3.0) * np.einsum("...ij,...kl->...ijkl", G, F)
+          + (2.0 / 9.0) * tr[..., None, None, None, None] * np.einsum("...ij,...kl->...ijkl", G, G)
+          + (1.0 / 3.0) * tr[..., None, None, None, None] * np.einsum("...il,...kj->...ijkl", G, G))
+    Jb = J[..., None, None, None, None]
+    t2 = ((2.0 * Jb - 1.0) * np.einsum("...ij,...kl->...ijkl", G, G)
+          + (1.0 - Jb) * np.einsum("...il,...kj->...ijkl", G, G))
+    return (mu / J23[..., None, None, None, None]) * t1 + kappa * Jb * t2
+
+
 # ---------------------------------------------------------------- stiffness from order parameters
 def _cells(eta, eta_lo, lo, hi, di, dj, dk):
     """eta over the nodal box [lo, hi] shifted by (di, dj, dk) cells: the array of
