@@ -95,7 +95,10 @@ inline double amax(double m, double v) {
 }
 
 // ---------------------------------------------------------------- Set::Matrix4 contractions
-int ncoef_of(int model) { return model == ORC_ISOTROPIC ? 2 : model == ORC_MAJORMINOR ? 21 : 9; }
+constexpr int kMaxCoef = 45;  // the largest kind: the Sym::Major tangent of a finite-kinematics model
+int ncoef_of(int model) {
+    return model == ORC_ISOTROPIC ? 2 : model == ORC_MAJORMINOR ? 21 : model == ORC_MAJOR ? 45 : 9;
+}
 
 // src/Set/Matrix4_MajorMinor.H:253-269 (stress of a 21-coefficient tensor)
 inline void stress_mm(const double* a, const double g[3][3], double s[3][3]) {
@@ -168,14 +171,42 @@ inline void div_diag(const double* a, const double b[3][3][3], double f[3]) {
         f[i] = r;
     }
 }
+// Set::Matrix4<3, Sym::Major> (src/Set/Matrix4_Major.H:198-300): the 9 x 9 matrix
+// A(3i+j, 3k+l) = C_ijkl is symmetric; its upper triangle is stored row by row (45 slots).
+inline int major_slot(int I, int K) {
+    if (I > K) { const int t = I; I = K; K = t; }
+    return I * 9 - I * (I - 1) / 2 + (K - I);
+}
+// src/Set/Matrix4_Major.H:399-413: sigma_ij = sum_kl C_ijkl g_kl, summed in (k, l) order
+inline void stress_major(const double* a, const double g[3][3], double s[3][3]) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double r = 0.0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) r += a[major_slot(3 * i + j, 3 * k + l)] * g[k][l];
+            s[i][j] = r;
+        }
+}
+// src/Set/Matrix4_Major.H:415-428: f_i = sum_{j,k,l} C_ijkl b[k][l][j], b[k][l][j] = u_{k,lj}
+inline void div_major(const double* a, const double b[3][3][3], double f[3]) {
+    for (int i = 0; i < 3; ++i) {
+        double r = 0.0;
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) r += a[major_slot(3 * i + j, 3 * k + l)] * b[k][l][j];
+        f[i] = r;
+    }
+}
 inline void stress_of(int model, const double* a, const double g[3][3], double s[3][3]) {
     if (model == ORC_ISOTROPIC) stress_iso(a, g, s);
     else if (model == ORC_MAJORMINOR) stress_mm(a, g, s);
+    else if (model == ORC_MAJOR) stress_major(a, g, s);
     else stress_diag(a, g, s);
 }
 inline void div_of(int model, const double* a, const double b[3][3][3], double f[3]) {
     if (model == ORC_ISOTROPIC) div_iso(a, b, f);
     else if (model == ORC_MAJORMINOR) div_mm(a, b, f);
+    else if (model == ORC_MAJOR) div_major(a, b, f);
     else div_diag(a, b, f);
 }
 
@@ -222,7 +253,7 @@ inline void fapply_node(const Lev& L, int model, const double* C, const int* bct
     const int nc = ncoef_of(model);
     int st[3];
     get_stencil(L, i, j, k, st);
-    double a[21];
+    double a[kMaxCoef];
     for (int q = 0; q < nc; ++q) a[q] = C[q * nn + c];
     double u[3], g[3][3];
     for (int p = 0; p < 3; ++p) {
@@ -257,7 +288,7 @@ inline void fapply_node(const Lev& L, int model, const double* C, const int* bct
         double col[3][3];
         for (int d = 0; d < 3; ++d) {
             const long o = L.stride(d);
-            double cg[21];
+            double cg[kMaxCoef];
             for (int q = 0; q < nc; ++q) {
                 const double* cq = C + q * nn + c;
                 if (st[d] == ST_LO) cg[q] = (cq[0] - cq[-o]) / L.dx[d];
@@ -296,7 +327,7 @@ void diagonal(const Lev& L, int model, const double* C, const int* bctype, doubl
         const bool xmin = i == L.dom.lo[0], ymin = j == L.dom.lo[1], zmin = k == L.dom.lo[2];
         const bool xmax = i == L.dom.hi[0], ymax = j == L.dom.hi[1], zmax = k == L.dom.hi[2];
         const bool mn[3] = {xmin, ymin, zmin}, mx[3] = {xmax, ymax, zmax};
-        double a[21];
+        double a[kMaxCoef];
         for (int q = 0; q < nc; ++q) a[q] = C[q * nn + c];
         double nrm[3];
         const int face = classify(L.dom, i, j, k, nrm);
@@ -323,7 +354,7 @@ void diagonal(const Lev& L, int model, const double* C, const int* bctype, doubl
                 div_of(model, a, b, f);
                 for (int d = 0; d < 3; ++d) {
                     const long o = L.stride(d);
-                    double cg[21];
+                    double cg[kMaxCoef];
                     for (int q = 0; q < nc; ++q) {
                         const double* cq = C + q * nn + c;
                         cg[q] = (cq[o] - cq[-o]) * 0.5 / L.dx[d];
@@ -857,7 +888,7 @@ int orc_stress(const orc_level* L, int model, const double* C, const double* U, 
         int st[3];
         get_stencil(l, i, j, k, st);
         const long c = l.at(i, j, k);
-        double g[3][3], s[3][3], a[21];
+        double g[3][3], s[3][3], a[kMaxCoef];
         for (int q = 0; q < nc; ++q) a[q] = C[q * l.nn + c];
         for (int p = 0; p < 3; ++p)
             for (int d = 0; d < 3; ++d) g[p][d] = D1(U + p * l.nn + c, l.stride(d), l.dx[d], st[d]);
@@ -882,7 +913,7 @@ int orc_energy(const orc_level* L, int model, const double* C, const double* U, 
         int st[3];
         get_stencil(l, i, j, k, st);
         const long c = l.at(i, j, k);
-        double g[3][3], s[3][3], a[21], e[3][3];
+        double g[3][3], s[3][3], a[kMaxCoef], e[3][3];
         for (int q = 0; q < nc; ++q) a[q] = C[q * l.nn + c];
         for (int p = 0; p < 3; ++p)
             for (int d = 0; d < 3; ++d) g[p][d] = D1(U + p * l.nn + c, l.stride(d), l.dx[d], st[d]);
@@ -1142,7 +1173,7 @@ inline void pgradC(const PLev& L, int model, const double* C, int i, int j, int 
     double col[3][3];
     for (int d = 0; d < 3; ++d) {
         const int o[3] = {d == 0, d == 1, d == 2};
-        double cg[21];
+        double cg[kMaxCoef];
         for (int q = 0; q < nc; ++q) {
             const PAt c{L, C + q * L.nn, i, j, k};
             cg[q] = (c(o[0], o[1], o[2]) - c(-o[0], -o[1], -o[2])) * 0.5 / L.dx[d];
@@ -1158,7 +1189,7 @@ inline void pfapply_node(const PLev& L, int model, const double* C, int uniform,
                          int k, double f[3]) {
     const long c = L.at(i, j, k);
     const int nc = ncoef_of(model);
-    double a[21];
+    double a[kMaxCoef];
     for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
     double g[3][3], b[3][3][3];
     pgrad(L, U, i, j, k, g, b);
@@ -1185,7 +1216,7 @@ void pdiagonal(const PLev& L, int model, const double* C, double* D) {
     const int nc = ncoef_of(model);
     for_cell(L, [&](int i, int j, int k) {
         const long c = L.at(i, j, k);
-        double a[21];
+        double a[kMaxCoef];
         for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
         for (int p = 0; p < 3; ++p) {
             double b[3][3][3] = {};
@@ -1515,7 +1546,7 @@ int orc_rve_mean_stress(const orc_rve_level* L0, int model, const double* C, con
         for (int j = 0; j < L.n[1]; ++j)
             for (int i = 0; i < L.n[0]; ++i) {
                 const long c = L.at(i, j, k);
-                double a[21], g[3][3], s[3][3];
+                double a[kMaxCoef], g[3][3], s[3][3];
                 for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
                 pgrad(L, w, i, j, k, g, nullptr);
                 for (int p = 0; p < 3; ++p)
@@ -1622,7 +1653,7 @@ inline void newton_grad(const Lev& L, const double* U, const int st[3], long c, 
 inline void newton_dw_node(const Lev& L, int model, const double* C, const double* F0, const double g[3][3], long c,
                            double sig[3][3]) {
     const int nc = ncoef_of(model);
-    double a[21], e[3][3];
+    double a[kMaxCoef], e[3][3];
     for (int q = 0; q < nc; ++q) a[q] = C[q * L.nn + c];
     for (int p = 0; p < 3; ++p)
         for (int d = 0; d < 3; ++d) e[p][d] = g[p][d] - (F0 ? F0[(3 * p + d) * L.nn + c] : 0.0);

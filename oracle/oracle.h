@@ -36,7 +36,10 @@ typedef struct {
 } orc_level;
 
 /* model kinds: per-node coefficient count in parentheses */
-enum { ORC_ISOTROPIC = 0 /* (lambda, mu) */, ORC_MAJORMINOR = 1 /* 21 */, ORC_DIAGONAL = 2 /* 9, A(i,j) row-major */ };
+enum {
+    ORC_ISOTROPIC = 0 /* (lambda, mu) */, ORC_MAJORMINOR = 1 /* 21 */, ORC_DIAGONAL = 2 /* 9, A(i,j) row-major */,
+    ORC_MAJOR = 3 /* 45: upper triangle of the symmetric 9 x 9 matrix C(3i+j, 3k+l), row by row */
+};
 
 /* BC types, same numbering as BC::Operator::Elastic<T>::Type (src/BC/Operator/Elastic.H:24) */
 enum { ORC_DISP = 0, ORC_TRAC = 1, ORC_PERIODIC = 2, ORC_NEUMANN = 3 };

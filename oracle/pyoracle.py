@@ -11,8 +11,8 @@ import numpy as np
 
 from . import build as _build
 
-ORC_ISOTROPIC, ORC_MAJORMINOR, ORC_DIAGONAL = 0, 1, 2
-NCOEF = {ORC_ISOTROPIC: 2, ORC_MAJORMINOR: 21, ORC_DIAGONAL: 9}
+ORC_ISOTROPIC, ORC_MAJORMINOR, ORC_DIAGONAL, ORC_MAJOR = 0, 1, 2, 3
+NCOEF = {ORC_ISOTROPIC: 2, ORC_MAJORMINOR: 21, ORC_DIAGONAL: 9, ORC_MAJOR: 45}
 
 
 class Level(C.Structure):
@@ -369,6 +369,37 @@ def neohookean_ddw(F, mu, kappa):
     t2 = ((2.0 * Jb - 1.0) * np.einsum("...ij,...kl->...ijkl", G, G)
           + (1.0 - Jb) * np.einsum("...il,...kj->...ijkl", G, G))
     return (mu / J23[..., None, None, None, None]) * t1 + kappa * Jb * t2
+
+
+def major45(ddw):
+    """Set::Matrix4<3, Sym::Major> storage (src/Set/Matrix4_Major.H:203-258) of tensors shaped
+    (..., 3, 3, 3, 3): the upper triangle of the 9 x 9 matrix A(3i+j, 3k+l), row by row; returned
+    as (45, ...) per-node coefficient fields.  Entries below the diagonal are taken from above
+    (the tensor is assumed major-symmetric)."""
+    ddw = np.asarray(ddw, dtype=np.float64)
+    A = ddw.reshape(ddw.shape[:-4] + (9, 9))
+    rows, cols = np.triu_indices(9)
+    return np.ascontiguousarray(np.moveaxis(A[..., rows, cols], -1, 0))
+
+
+def neohookean_newton(L, mu, kappa, bctype, u, b, nriters=6, tol_rel=1e-10, tol_abs=0.0, **kw):
+    """Solver::Nonlocal::Newton<NeoHookean>::solve restated (src/Solver/Nonlocal/Newton.H:142-209):
+    each iteration forms rhs = b - N(u) and the tangent DDW(I + grad u) node by node
+    (prepareForSolve), solves the tangent operator for the correction starting from the previous
+    correction (the reference never resets it), and adds it to u.  Returns (u, [max |correction|
+    per iteration])."""
+    u = np.array(u, dtype=np.float64, copy=True)
+    du = np.zeros_like(u)
+    hist = []
+    for _ in range(nriters):
+        rhs, ddw = neohookean_newton_residual(L, mu, kappa, bctype, u, b)
+        C = major45(ddw)
+        du, st, rc = solve(L, ORC_MAJOR, C, bctype, du, rhs, tol_rel, tol_abs, **kw)
+        if rc != 0:
+            raise RuntimeError("tangent solve did not converge")
+        hist.append(float(np.abs(du).max()))
+        u += du
+    return u, hist
 
 
 # ---------------------------------------------------------------- stiffness from order parameters

@@ -98,3 +98,73 @@ def test_neohookean_homogeneous_deformation_is_in_equilibrium_inside():
     b = np.zeros_like(u)
     rhs, _ = po.neohookean_newton_residual(L, MU, KAPPA, np.zeros((26, 3), np.int32), u, b)
     assert np.abs(rhs[:, 1:-1, 1:-1, 1:-1]).max() < 1e-12
+
+
+def iso_tensor(lam, mu):
+    I = np.eye(3)
+    return (lam[..., None, None, None, None] * np.einsum("ij,kl->ijkl", I, I)
+            + mu[..., None, None, None, None] * (np.einsum("ik,jl->ijkl", I, I) + np.einsum("il,jk->ijkl", I, I)))
+
+
+def test_major_kind_reproduces_the_isotropic_operator():
+    """The 45-slot Sym::Major kind, filled with the isotropic tensor node by node, gives the
+    isotropic operator's Fapply and Diagonal (∇C term and BC rows included)."""
+    from helpers import bc_random
+    rng = np.random.default_rng(5)
+    L = po.level((8, 6, 10))
+    lam = 1.0 + rng.random(L.shape)
+    mu = 0.5 + rng.random(L.shape)
+    Ciso = np.ascontiguousarray(np.stack([lam, mu]))
+    C45 = po.major45(iso_tensor(lam, mu))
+    assert C45.shape == (45,) + L.shape
+    bc = bc_random(rng)
+    u = rng.standard_normal((3,) + L.shape)
+    ref = po.fapply(L, po.ORC_ISOTROPIC, Ciso, bc.type, u)
+    got = po.fapply(L, po.ORC_MAJOR, C45, bc.type, u)
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    dref = po.diagonal(L, po.ORC_ISOTROPIC, Ciso, bc.type)
+    dgot = po.diagonal(L, po.ORC_MAJOR, C45, bc.type)
+    assert np.abs(dgot - dref).max() <= 1e-13 * np.abs(dref).max()
+
+
+def test_major45_layout_is_the_reference_table():
+    """Spot checks of the slot table of Matrix4<3, Sym::Major>::operator() (Matrix4_Major.H:203-258):
+    slot 1 holds C_0001 = C_0100, slot 11 C_0110 = C_1001, slot 24 C_1010, slot 44 C_2222."""
+    T = np.zeros((3, 3, 3, 3))
+    for idx, v in [((0, 0, 0, 1), 1.0), ((0, 1, 1, 0), 2.0), ((1, 0, 1, 0), 3.0), ((2, 2, 2, 2), 4.0)]:
+        T[idx] = v
+        T[idx[2], idx[3], idx[0], idx[1]] = v
+    c = po.major45(T)
+    assert (c[1], c[11], c[24], c[44]) == (1.0, 2.0, 3.0, 4.0)
+    assert np.count_nonzero(c) == 4
+
+
+def test_neohookean_newton_uniaxial_known_answer():
+    """Uniaxial stretch of a NeoHookean block with symmetry rollers on the low faces, x = 1 pulled
+    to 1 + d and the rest traction-free: the exact solution is homogeneous, F = diag(s, t, t) with
+    P_yy(F) = 0, and the nodal operator reproduces affine fields exactly, so Newton must land on
+    it, with the corrections falling quadratically."""
+    from scipy.optimize import brentq
+    from helpers import bc_config0  # noqa: F401  (helpers on the path)
+    from anisotropicfracture_gb300.elastic import FACES
+    D_, T_ = 0, 1
+    d = 0.1
+    s = 1.0 + d
+    t = brentq(lambda t: po.neohookean_dw(np.diag([s, t, t]), MU, KAPPA)[1, 1], 0.5, 1.5)
+    L = po.level(4)
+    bt = np.full((26, 3), T_, np.int32)
+    bv = np.zeros((26, 3))
+    for f, name in enumerate(FACES):
+        for p, ax in enumerate("XYZ"):
+            if ax + "LO" in name:
+                bt[f, p] = D_
+            elif ax == "X" and "XHI" in name:
+                bt[f, p], bv[f, p] = D_, d
+    b = po.bc_init(L, bt, bv, np.zeros((3,) + L.shape))
+    u, hist = po.neohookean_newton(L, MU, KAPPA, bt, np.zeros_like(b), b, nriters=7, tol_rel=1e-12,
+                                   max_fmg_iter=100000000, bottom=1, nu1=2, nu2=2)
+    X, Y, Z = po.node_coords(L)
+    exact = np.stack([(s - 1) * X, (t - 1) * Y, (t - 1) * Z])
+    assert np.abs(u - exact).max() < 1e-9
+    assert hist[3] < 1e-6 and hist[-1] < 1e-10
+    assert hist[2] < hist[1] ** 1.5 * 10  # quadratic convergence, loosely
