@@ -73,3 +73,37 @@ def test_host_only_entry_points(lib):
     assert lib.ae_op_create(None, 0, 0, C.byref(h)) == _lib.AE_ERR_ARG
     assert b"level" in lib.ae_last_error()
     assert lib.ae_op_num_amr_levels(None) == 0
+
+
+def _levels(*descs):
+    arr = (_lib.LevelDesc * len(descs))()
+    for a, (cells, lo, hi, dx) in enumerate(descs):
+        for d in range(3):
+            arr[a].domain_cells[d], arr[a].lo[d], arr[a].hi[d], arr[a].dx[d] = cells, lo, hi, dx
+    return arr
+
+
+@pytest.mark.parametrize("descs,model,what", [
+    ([(8, 0, 8, 0.125)], 3, b"model"),                                   # unknown stiffness kind
+    ([(8, 0, 8, 0.0)], 0, b"dx"),                                        # non-positive spacing
+    ([(8, 0, 9, 0.125)], 0, b"outside"),                                 # patch beyond the domain
+    ([(8, 2, 8, 0.125)], 0, b"whole domain"),                            # level 0 must cover it
+    ([(8, 0, 8, 0.125), (12, 4, 8, 0.0625)], 0, b"refine by 2"),         # refinement ratio
+    ([(8, 0, 8, 0.125), (16, 3, 9, 0.0625)], 0, b"align"),               # odd fine patch corners
+])
+def test_level_descriptions_are_checked_on_the_host(lib, descs, model, what):
+    """Operator::Elastic<T>::define's preconditions (src/Operator/Elastic.cpp:30-55) are checked
+    before any device work, with the reference's Util::Abort turned into AE_ERR_ARG."""
+    h = C.c_void_p()
+    assert lib.ae_op_create(_levels(*descs), len(descs), model, C.byref(h)) == _lib.AE_ERR_ARG
+    assert what in lib.ae_last_error()
+    assert not h.value
+
+
+def test_null_handles_are_argument_errors(lib):
+    fab = _lib.Fab()
+    assert lib.ae_op_set_model(None, 0, C.byref(fab)) == _lib.AE_ERR_ARG
+    assert lib.ae_op_set_model_mixture(None, 0, C.byref(fab), 1, None, None, None) == _lib.AE_ERR_ARG
+    assert lib.ae_op_set_model_degraded(None, 0, None, 0, 1.0, 1.0) == _lib.AE_ERR_ARG
+    assert lib.ae_fapply(None, 0, 0, C.byref(fab), C.byref(fab)) == _lib.AE_ERR_ARG
+    assert b"null" in lib.ae_last_error()
