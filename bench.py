@@ -57,7 +57,7 @@ JACOBI32_TRAFFIC_PER_NODE = {True: 47.3, False: 131.1}
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
 # time to a full solve in the reference arm, which cannot afford a full CPU solve.
-CONFIG1_FP64_ITERS = int(os.environ.get("AE_CONFIG1_ITERS", "0"))
+FP64_ITERS_OVERRIDE = int(os.environ.get("AE_FP64_ITERS", "0"))
 
 
 def workload(n=256, nseeds=64, seed_points=1, seed_rot=2):
@@ -237,7 +237,7 @@ def run_reference(args, rank):
     if rank != 0:
         return
     levels, bc = workload(args.cells)
-    iters = CONFIG1_FP64_ITERS or args.ref_iters
+    iters = FP64_ITERS_OVERRIDE or args.ref_iters
     rhs = [oracle_rhs(L, bc) for L in levels]
     samples = []
     for k in range(args.warmup + args.steps):
@@ -256,14 +256,14 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-# ---------------------------------------------------------------- config 2: damaged polycrystal
-def bench_config2(args):
+# ---------------------------------------------------------------- damaged polycrystal, 193^3 nodes
+def bench_damaged_polycrystal(args):
     """Phase-field-degraded cubic polycrystal, single level, mixed vs FP64 and the displacement error.
     The stiffness floor of g(c) = (1-c)^2 + floor is args.damage_floor (see the returned note)."""
     import torch
     from anisotropicfracture_gb300 import microstructure, models
     from anisotropicfracture_gb300.elastic import BCElastic, Elastic, FACES, Field, Linear, level_desc
-    n = args.config2_cells
+    n = args.damaged_cells
     dx = (1.0 / n,) * 3
     C, _, _ = microstructure.cubic_polycrystal((0, 0, 0), (n, n, n), dx, nseeds=64, seed_points=1, seed_rot=2)
     c = microstructure.penny_crack_damage((0, 0, 0), (n, n, n), dx, ncracks=8, seed=3, width_cells=3.0,
@@ -588,7 +588,7 @@ def main():
     ap.add_argument("--mixed-tight-tol", type=float, default=0.0,
                     help="also time the mixed solve to this residual and report its error (0: off)")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    # composite FP64 iterations of the config-1 solve: measured by this benchmark's FP64 solve
+    # composite FP64 iterations of the two-level 257^3 polycrystal solve: measured by this benchmark's FP64 solve
     # (167), which follows the oracle iteration for iteration
     ap.add_argument("--ref-iters", type=int, default=167)
     ap.add_argument("--cpu-sample-iters", type=int, default=1)
@@ -600,8 +600,8 @@ def main():
                     help="FP32 cycles per FP64 residual in mixed precision")
     ap.add_argument("--per-node-model", action="store_true",
                     help="give the single-box stiffness per node (ae_op_set_model) instead of as grain ids + table")
-    ap.add_argument("--no-config2", action="store_true", help="skip the damaged-polycrystal workload")
-    ap.add_argument("--config2-cells", type=int, default=192)
+    ap.add_argument("--no-damaged", action="store_true", help="skip the damaged-polycrystal workload")
+    ap.add_argument("--damaged-cells", type=int, default=192)
     ap.add_argument("--damage-floor", type=float, default=0.1,
                     help="stiffness floor of g(c) in the damaged workload (the specified 1e-6 diverges)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cell workload")
@@ -924,11 +924,11 @@ def add_cell_workloads(args, lib, line, rank, world):
             line["batch"] = {"error": str(e)}
     if world > 1 or rank != 0:
         return
-    if not args.no_config2:
+    if not args.no_damaged:
         try:
-            line["config2"] = bench_config2(args)
+            line["damaged_polycrystal"] = bench_damaged_polycrystal(args)
         except Exception as e:  # pragma: no cover
-            line["config2"] = {"error": str(e)}
+            line["damaged_polycrystal"] = {"error": str(e)}
     if not args.no_serve:
         try:
             line["serve"] = bench_serve(args)

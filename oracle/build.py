@@ -1,7 +1,7 @@
 """Build recipe for the CPU FP64 oracle (test infrastructure only).
 
 Compiles oracle/oracle.cpp into oracle/_build/liboracle.so with g++ and OpenMP.
-The oracle is the checker for the CUDA library; nothing in the product links it.
+The oracle is the parity reference for the CUDA library; nothing in the product links it.
 """
 import os
 import subprocess

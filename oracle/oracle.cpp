@@ -1,6 +1,6 @@
 // CPU FP64 restatement of the reference's nodal elastic operator path and of the
-// AMReX MLMG cycle around it.  TEST INFRASTRUCTURE ONLY: the checker for the CUDA
-// library, loaded by tests/, the smoke check and bench.py's cpu_baseline leg.
+// AMReX MLMG cycle around it.  TEST INFRASTRUCTURE ONLY: the parity reference for the
+// CUDA library, loaded by tests/, the smoke check and bench.py's cpu_baseline leg.
 //
 // Every function cites the reference lines it restates.  Arithmetic follows the
 // reference's expression order; the build uses -ffp-contract=off so that no

@@ -4,8 +4,8 @@
  * Numeric::Stencil, Set::Matrix4 contractions) and of the AMReX MLMG cycle that
  * drives it.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker: tests/, the smoke
- * check and bench.py's cpu_baseline leg may load it; the product (the CUDA
+ * TEST INFRASTRUCTURE ONLY: the parity reference for the CUDA library. tests/, the
+ * smoke check and bench.py's cpu_baseline leg may load it; the product (the CUDA
  * library under anisotropicfracture_gb300/csrc) never links or calls it.
  *
  * Pinning: the reference ships no golden vectors and cannot be built here

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU FP64 oracle (test infrastructure only).
 
 Only tests/, the smoke check and bench.py's cpu_baseline leg import this module,
-and only as the checker.  Fields are numpy float64 arrays shaped
+and only as the parity reference.  Fields are numpy float64 arrays shaped
 (ncomp, nz, ny, nx) over the stored box grow(valid, ng), i fastest.
 """
 import ctypes as C

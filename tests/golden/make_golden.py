@@ -15,7 +15,7 @@ Inputs are multiples of 1/64 (exact in FP32 and FP64, small when compressed).  E
   resid    = b - Fapply(x), and its max-norm          src/Operator/Operator.cpp:842-852
   restrict = Operator<Node>::restriction(u)             src/Operator/Operator.cpp:454-554
   interp   = x + Operator<Node>::interpolation(crse)     src/Operator/Operator.cpp:556-624
-  solve_u, solve_iters: V-cycle solve of the config-0 problem from zero to 1e-8
+  solve_u, solve_iters: V-cycle solve of the pull-along-z problem from zero to 1e-8
 
 Regenerate with:  python tests/golden/make_golden.py
 """
@@ -29,7 +29,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, os.path.dirname(HERE))
 
 from anisotropicfracture_gb300 import models  # noqa: E402
-from helpers import bc_config0, golden_stiffness  # noqa: E402
+from helpers import bc_pull_z, golden_stiffness  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
 
 OUT = os.path.join(HERE, "elastic_ops.npz")
@@ -89,11 +89,11 @@ def make():
                     p + "resid": r, p + "resid_norm": np.float64(rn),
                     p + "restrict": po.restrict(Lc, L, u),
                     p + "interp": po.interp_add(L, Lc, x, crse)})
-    # a V-cycle solve of the config-0 problem (u = 0 on z = 0, u_z = 0.01 on z = 1) on 4 grains
+    # a V-cycle solve of the pull-along-z problem (u = 0 on z = 0, u_z = 0.01 on z = 1) on 4 grains
     rng = np.random.default_rng(2000)
     L = po.level(SOLVE_CELLS)
     C, parts = coeffs(models.MAJORMINOR, L.shape, rng)
-    bc = bc_config0()
+    bc = bc_pull_z()
     b = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
     u, st, rc = po.solve(L, models.MAJORMINOR, C, bc.type, np.zeros_like(b), b, 1e-8, 0.0)
     assert rc == 0

@@ -23,8 +23,8 @@ def random_coeffs(model, shape, rng, smooth=False):
     return np.ascontiguousarray(C)
 
 
-def bc_config0():
-    """Config 0 BCs: u = 0 on z = 0, u = (0, 0, 0.01) on z = 1, traction-free lateral faces;
+def bc_pull_z():
+    """Pull along z: u = 0 on z = 0, u = (0, 0, 0.01) on z = 1, traction-free lateral faces;
     edges and corners touching z = 0 / z = 1 take the z-face type."""
     bc = BCElastic()
     for f in FACES:
@@ -79,11 +79,11 @@ def normwise_err(a, ref):
 
 def polycrystal_amr(n=16, nlev=2, seed=1):
     """The reference's test hierarchy (oracle amr_levels) with an 8-grain cubic Voronoi stiffness
-    on every level (ghost nodes included) and the config-0 boundary values as right-hand sides."""
+    on every level (ghost nodes included) and the pull-along-z boundary values as right-hand sides."""
     from anisotropicfracture_gb300 import microstructure
     from oracle import pyoracle as po
     Ls = po.amr_levels(n, nlev)
-    bc = bc_config0()
+    bc = bc_pull_z()
     seeds = microstructure.voronoi_seeds(8, seed)
     rot = models.random_rotations(8, np.random.default_rng(seed + 1))
     tab = models.cubic(1.68, 1.21, 0.75, rot)

@@ -11,7 +11,7 @@ import pytest
 
 from anisotropicfracture_gb300 import _lib, microstructure, models
 from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
-from helpers import bc_config0, bc_random
+from helpers import bc_pull_z, bc_random
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
@@ -92,7 +92,7 @@ def test_grain_kernels_equal_per_node_kernels(precision):
 def test_grain_solves_equal_per_node_solves(precision, nlev):
     Ls = po.amr_levels(16, nlev)
     gids, Cs, tab = _poly(Ls, ngr=10, seed=7)
-    bc = bc_config0()
+    bc = bc_pull_z()
     bs = [po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape)) for L in Ls]
     a, b = _ops(Ls, bc, gids, Cs, tab)
     outs = []

@@ -5,7 +5,7 @@ import pytest
 
 from anisotropicfracture_gb300 import models
 from anisotropicfracture_gb300.elastic import Elastic, Field, Newton, level_desc
-from helpers import bc_config0, bc_random, normwise_err, random_coeffs
+from helpers import bc_pull_z, bc_random, normwise_err, random_coeffs
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
@@ -90,7 +90,7 @@ def test_eigenstrain_newton_solve_matches_oracle():
     F0 = np.zeros((9,) + L.shape)
     for q in (0, 4, 8):
         F0[q] = 0.01 * inside
-    bc = bc_config0()
+    bc = bc_pull_z()
     b = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
     rhs = po.newton_residual(L, po.ORC_ISOTROPIC, Cf, bc.type, np.zeros_like(b), b, F0=F0)
     ref, st, rc = po.solve(L, po.ORC_ISOTROPIC, Cf, bc.type, np.zeros_like(b), rhs, 1e-10, 0.0, bottom=0, nu1=2,

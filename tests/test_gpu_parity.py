@@ -8,7 +8,7 @@ import pytest
 
 from anisotropicfracture_gb300 import models
 from anisotropicfracture_gb300.elastic import BCElastic, Elastic, Field, level_desc
-from helpers import bc_config0, bc_random, normwise_err, random_coeffs
+from helpers import bc_pull_z, bc_random, normwise_err, random_coeffs
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
@@ -33,7 +33,7 @@ def make_case(model, cells, bckind, uniform, seed, dx=None):
     cells = (cells,) * 3 if np.isscalar(cells) else tuple(cells)
     L = po.level(cells, dx=dx)
     Cf = random_coeffs(model, L.shape, rng)
-    bc = {"disp": BCElastic(), "config0": bc_config0(), "random": bc_random(rng)}[bckind]
+    bc = {"disp": BCElastic(), "pull_z": bc_pull_z(), "random": bc_random(rng)}[bckind]
     op = Elastic([level_desc(cells, dx=dx)], model)
     op.SetModel(0, Field(Cf))
     op.SetBC(bc)
@@ -43,7 +43,7 @@ def make_case(model, cells, bckind, uniform, seed, dx=None):
 
 
 CASES = [(m, n, bck, uni) for m in MODELS for (n, bck, uni) in
-         [(8, "random", False), (9, "config0", False), (16, "random", True), ((8, 6, 10), "random", False)]]
+         [(8, "random", False), (9, "pull_z", False), (16, "random", True), ((8, 6, 10), "random", False)]]
 
 
 @pytest.mark.parametrize("model,cells,bckind,uniform", CASES)
@@ -68,7 +68,7 @@ def test_fapply_fp32_matches_oracle(model):
 
 
 @pytest.mark.parametrize("model", MODELS)
-@pytest.mark.parametrize("bckind", ["random", "config0"])
+@pytest.mark.parametrize("bckind", ["random", "pull_z"])
 def test_diagonal_all_levels(model, bckind):
     """Diagonal on every multigrid level; coarse stiffness from the oracle's restriction
     (averageDownCoeffsSameAmrLevel)."""
@@ -93,7 +93,7 @@ def test_diagonal_all_levels(model, bckind):
 @pytest.mark.parametrize("model", MODELS)
 @pytest.mark.parametrize("nsweeps", [1, 2])
 def test_fsmooth_matches_oracle(model, nsweeps):
-    rng, L, Cf, bc, op = make_case(model, 16, "config0", False, 31)
+    rng, L, Cf, bc, op = make_case(model, 16, "pull_z", False, 31)
     x = rng.standard_normal((3,) + L.shape)
     b = rng.standard_normal((3,) + L.shape)
     xd = dev(x)
@@ -158,7 +158,7 @@ def test_strain_stress_energy(model):
 def test_fab_with_ghosts_and_offsets():
     """Fields may carry ghost nodes (AMReX fabs with nGrow = 2): the operator reads and
     writes through the fab's own box."""
-    rng, L, Cf, bc, op = make_case(models.MAJORMINOR, 8, "config0", False, 81)
+    rng, L, Cf, bc, op = make_case(models.MAJORMINOR, 8, "pull_z", False, 81)
     u = rng.standard_normal((3,) + L.shape)
     ug = np.zeros((3, 13, 13, 13))
     ug[:, 2:-2, 2:-2, 2:-2] = u
@@ -179,7 +179,7 @@ def tiled64(monkeypatch):
 
 
 @pytest.mark.parametrize("model", MODELS)
-@pytest.mark.parametrize("cells,bckind,uniform", [(16, "random", False), (33, "config0", False),
+@pytest.mark.parametrize("cells,bckind,uniform", [(16, "random", False), (33, "pull_z", False),
                                                   ((40, 9, 20), "random", True)])
 def test_tiled64_fapply_fsmooth(tiled64, model, cells, bckind, uniform):
     """The tiled kernel (FP64 instantiation) matches the oracle at 1e-12, including tile edges
@@ -227,7 +227,7 @@ def test_tiled64_fine_patch_with_ghosts(tiled64, model):
 @pytest.mark.parametrize("model", MODELS)
 def test_fsmooth_fp32_tiled(model, monkeypatch):
     monkeypatch.setenv("AE_TILED32", "1")
-    rng, L, Cf, bc, op = make_case(model, 24, "config0", False, 91)
+    rng, L, Cf, bc, op = make_case(model, 24, "pull_z", False, 91)
     x = rng.standard_normal((3,) + L.shape).astype(np.float32)
     b = rng.standard_normal((3,) + L.shape).astype(np.float32)
     xd = dev(x)

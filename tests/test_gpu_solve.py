@@ -6,18 +6,18 @@ import pytest
 from anisotropicfracture_gb300 import _lib, microstructure, models
 from anisotropicfracture_gb300._lib import AeError
 from anisotropicfracture_gb300.elastic import BCElastic, Elastic, Field, Linear, level_desc
-from helpers import bc_config0, bc_uniaxial_x, normwise_err, random_coeffs
+from helpers import bc_pull_z, bc_uniaxial_x, normwise_err, random_coeffs
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def config0_problem(n):
-    """Config 0 at n cells: isotropic sphere inclusion (E 10 / 1, nu 0.3), config-0 BCs."""
+def sphere_inclusion_problem(n):
+    """n^3 cells: isotropic sphere inclusion (E 10 / 1, nu 0.3), pulled along z."""
     L = po.level(n)
     Cf = microstructure.sphere_inclusion_iso((0, 0, 0), (n, n, n), (1.0 / n,) * 3)
-    bc = bc_config0()
+    bc = bc_pull_z()
     b = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
     return L, Cf, bc, b
 
@@ -39,8 +39,8 @@ def gpu_solver(n, model, Cf, bc, fmg=0, bottom=0, nu=1, precision="fp64", **kw):
 
 @pytest.mark.parametrize("n", [16, 32])
 @pytest.mark.parametrize("fmg,bottom,nu", [(0, 0, 1), (100000000, 1, 2)])
-def test_config0_fp64_matches_oracle(n, fmg, bottom, nu):
-    L, Cf, bc, b = config0_problem(n)
+def test_sphere_inclusion_fp64_matches_oracle(n, fmg, bottom, nu):
+    L, Cf, bc, b = sphere_inclusion_problem(n)
     ref, st, rc = po.solve(L, po.ORC_ISOTROPIC, Cf, bc.type, np.zeros_like(b), b, 1e-8, 0.0,
                            max_fmg_iter=fmg, bottom=bottom, nu1=nu, nu2=nu)
     assert rc == 0
@@ -53,10 +53,10 @@ def test_config0_fp64_matches_oracle(n, fmg, bottom, nu):
     assert normwise_err(x, ref) < 1e-8
 
 
-def test_config0_mixed_precision_error():
+def test_sphere_inclusion_mixed_precision_error():
     """FP32 cycle inside FP64 refinement: 1e-8 residual, displacement within 1e-7 of the FP64 oracle."""
     n = 32
-    L, Cf, bc, b = config0_problem(n)
+    L, Cf, bc, b = sphere_inclusion_problem(n)
     ref, st, rc = po.solve(L, po.ORC_ISOTROPIC, Cf, bc.type, np.zeros_like(b), b, 1e-10, 0.0)
     op, s = gpu_solver(n, models.ISOTROPIC, Cf, bc, precision="mixed")
     x = np.zeros_like(b)
@@ -69,7 +69,7 @@ def test_polycrystal_fp64_and_mixed():
     n = 16
     L = po.level(n)
     Cf, gid, tab = microstructure.cubic_polycrystal((0, 0, 0), (n, n, n), (1.0 / n,) * 3, nseeds=8)
-    bc = bc_config0()
+    bc = bc_pull_z()
     b = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
     ref, st, rc = po.solve(L, po.ORC_MAJORMINOR, Cf, bc.type, np.zeros_like(b), b, 1e-8, 0.0)
     assert rc == 0
@@ -116,7 +116,7 @@ def test_uniaxial_known_answer_on_gpu():
 
 def test_host_and_device_buffers_agree():
     n = 16
-    L, Cf, bc, b = config0_problem(n)
+    L, Cf, bc, b = sphere_inclusion_problem(n)
     op, s = gpu_solver(n, models.ISOTROPIC, Cf, bc)
     xh = np.zeros_like(b)
     s.solve(Field(xh), Field(b), 1e-8, 0.0)
@@ -128,7 +128,7 @@ def test_host_and_device_buffers_agree():
 
 def test_graph_and_eager_agree():
     n = 16
-    L, Cf, bc, b = config0_problem(n)
+    L, Cf, bc, b = sphere_inclusion_problem(n)
     op, s = gpu_solver(n, models.ISOTROPIC, Cf, bc, use_graph=1)
     xg = np.zeros_like(b)
     s.solve(Field(xg), Field(b), 1e-8, 0.0)
@@ -140,7 +140,7 @@ def test_graph_and_eager_agree():
 
 def test_error_behaviour():
     n = 8
-    L, Cf, bc, b = config0_problem(n)
+    L, Cf, bc, b = sphere_inclusion_problem(n)
     op, s = gpu_solver(n, models.ISOTROPIC, Cf, bc, max_iter=1)
     x = np.zeros_like(b)
     with pytest.raises(AeError) as e:

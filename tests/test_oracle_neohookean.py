@@ -145,7 +145,6 @@ def test_neohookean_newton_uniaxial_known_answer():
     P_yy(F) = 0, and the nodal operator reproduces affine fields exactly, so Newton must land on
     it, with the corrections falling quadratically."""
     from scipy.optimize import brentq
-    from helpers import bc_config0  # noqa: F401  (helpers on the path)
     from anisotropicfracture_gb300.elastic import FACES
     D_, T_ = 0, 1
     d = 0.1
