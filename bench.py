@@ -60,6 +60,12 @@ JACOBI32_TRAFFIC_PER_NODE = {True: 47.3, False: 131.1}
 FP64_ITERS_OVERRIDE = int(os.environ.get("AE_FP64_ITERS", "0"))
 
 
+def workload_label(n):
+    """The workload both arms report in config.workload."""
+    return ("polycrystal 2-level AMR: %d^3 cells + ratio-2 patch over the central 1/8 (2 x %d^3 nodes), "
+            "cubic 1.68/1.21/0.75, 64 Voronoi grains" % (n, n + 1))
+
+
 def workload(n=256, nseeds=64, seed_points=1, seed_rot=2):
     """Levels, stiffness and right-hand sides of the two-level polycrystal (host arrays)."""
     from anisotropicfracture_gb300 import microstructure, models
@@ -249,7 +255,7 @@ def run_reference(args, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "polycrystal 2-level AMR, 257^3 + 257^3-node patch, cubic 64 grains",
+            "config": {"workload": workload_label(args.cells),
                        "precision": "fp64", "cycle": "V(2,2) Jacobi, CG bottom", "tol_rel": 1e-8},
             "cpu_baseline": dict(cb, value=v),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -872,8 +878,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "polycrystal 2-level AMR: 256^3 cells + ratio-2 patch over the central 1/8 "
-                               "(2 x 257^3 nodes), cubic 1.68/1.21/0.75, 64 Voronoi grains",
+        "config": {"workload": workload_label(args.cells),
                    "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, CG bottom", "tol_rel": 1e-8,
                    "precision": "mixed: FP32 cycle in FP64 refinement", "inner_cycles": args.inner,
                    "stiffness": ("per-node coefficients (ae_op_set_model)" if args.per_node_model else
