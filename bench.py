@@ -612,6 +612,8 @@ def main():
                     help="stiffness floor of g(c) in the damaged workload (the specified 1e-6 diverges)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cell workload")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-cell workload")
+    ap.add_argument("--no-builders", action="store_true",
+                    help="skip timing the device-side model builders (mixture, degradation)")
     ap.add_argument("--only-cells", action="store_true", help="run only the batched/served cell workloads")
     ap.add_argument("--batch-cells", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2)
@@ -939,6 +941,60 @@ def add_cell_workloads(args, lib, line, rank, world):
             line["serve"] = bench_serve(args)
         except Exception as e:  # pragma: no cover
             line["serve"] = {"error": str(e)}
+    if not args.no_builders:
+        try:
+            line["model_builders"] = bench_model_builders(args)
+        except Exception as e:  # pragma: no cover
+            line["model_builders"] = {"error": str(e)}
+
+
+def bench_model_builders(args, reps=5):
+    """The per-node stiffness built on the device from cell-centred order parameters over the
+    (cells+1)^3 nodes of the single-box workload: the phase-field mixture of two cubic phases with
+    eigenstrains (ae_op_set_model_mixture) and the isotropic degradation (ae_op_set_model_degraded).
+    Inputs and outputs resident on the device; host clock around the call, which synchronises.
+    Algorithmic bytes per node: mixture 21 slots + 9 eigenstrain written + one cell per phase read
+    = 8 (21 + 9 + 2) = 256; degradation 2 slots written + one cell read = 24."""
+    import torch
+    from anisotropicfracture_gb300 import models
+    from anisotropicfracture_gb300.elastic import Elastic, Field, level_desc
+    n = args.cells
+    nodes = (n + 1) ** 3
+    rng = np.random.default_rng(7)
+    torch.manual_seed(7)
+    out = {"nodes": nodes, "timing": "host clock around %d synchronous calls, after one warm-up call" % reps}
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps
+
+    eta = 0.05 + torch.rand((2, n + 1, n + 2, n + 2), dtype=torch.float64, device="cuda")
+    table = models.cubic(1.68, 1.21, 0.75, models.random_rotations(2, rng))
+    F0table = 0.01 * rng.standard_normal((2, 9))
+    F0 = torch.zeros((9, n + 1, n + 1, n + 1), dtype=torch.float64, device="cuda")
+    op = Elastic([level_desc(n)], models.MAJORMINOR)
+    try:
+        ms = timed(lambda: op.SetModelMixture(0, Field(eta, (-1, -1, 0)), table, F0table, Field(F0)))
+    finally:
+        op.close()
+    del eta, F0
+    out["mixture"] = {"ms": ms, "bytes_per_node": 256, "GB/s": 256.0 * nodes / (ms * 1e-3) / 1e9}
+
+    damage = 0.9 * torch.rand((1, n + 2, n + 2, n + 2), dtype=torch.float64, device="cuda")
+    op = Elastic([level_desc(n)], models.ISOTROPIC)
+    try:
+        ms = timed(lambda: op.SetModelDegraded(0, Field(damage, (-1, -1, -1)), 2.0, 1.0))
+    finally:
+        op.close()
+    del damage
+    torch.cuda.empty_cache()
+    out["degraded"] = {"ms": ms, "bytes_per_node": 24, "GB/s": 24.0 * nodes / (ms * 1e-3) / 1e9}
+    return out
 
 
 def main_cells_only(args):
