@@ -12,6 +12,7 @@
 
 #include <array>
 #include <cmath>
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -65,6 +66,31 @@ struct Level {
         return L;
     }
 };
+
+// Integrator::WritePlotFile, node half (src/Integrator/Integrator.cpp:582-681): writes
+// <plot_file>/<step:05d>[init]node as an AMReX plotfile (one host fab per level, the named
+// components on its valid box) and appends its Header to <plot_file>/nodeoutput.visit, which
+// step 0 creates.  Returns the plotfile directory.
+inline std::string WritePlotFile(const std::string& plot_file, int step, const std::vector<Level>& levels,
+                                 const std::vector<Fab>& fabs, const std::vector<std::string>& names,
+                                 double time, bool initial = false) {
+    std::vector<ae_level_desc> d;
+    std::vector<ae_fab> f;
+    for (const auto& L : levels) d.push_back(L.c());
+    for (const auto& x : fabs) f.push_back(x.c());
+    std::vector<const char*> cn;
+    for (const auto& n : names) cn.push_back(n.c_str());
+    char num[16];
+    std::snprintf(num, sizeof(num), "%05d", step);
+    const std::string name = std::string(num) + (initial ? "init" : "") + "node";
+    const std::string dir = plot_file + "/" + name;
+    check(ae_write_plotfile(dir.c_str(), (int)d.size(), d.data(), f.data(), (int)cn.size(), cn.data(), time, nullptr));
+    std::FILE* visit = std::fopen((plot_file + "/nodeoutput.visit").c_str(), step == 0 ? "w" : "a");
+    if (!visit) throw Error(AE_ERR_STATE, "cannot write " + plot_file + "/nodeoutput.visit");
+    std::fprintf(visit, "%s/Header\n", name.c_str());
+    std::fclose(visit);
+    return dir;
+}
 
 }  // namespace alamo
 

@@ -38,3 +38,22 @@ def test_shim_uniaxial_solve():
     r = subprocess.run([exe, "32"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert '"converged": 1' in r.stdout
+
+
+def test_shim_writes_a_plotfile_without_a_gpu(tmp_path):
+    """alamo::WritePlotFile (host fabs only) from C++: the reference's directory naming and .visit
+    list, and the valid-box values of each level read back."""
+    from anisotropicfracture_gb300 import plotfile
+    build.build()
+    exe = _compile("plotfile_shim.cpp", "plotfile_shim", link=True)
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip() == str(tmp_path / "00003node")
+    with open(tmp_path / "nodeoutput.visit") as f:
+        assert f.read() == "00000node/Header\n00003node/Header\n"
+    p = plotfile.read_plotfile(str(tmp_path / "00003node"))
+    assert p["time"] == 1.5 and p["names"] == ["disp001", "disp002", "disp003"]
+    for lev, (lo, hi) in zip(p["levels"], [((0, 0, 0), (8, 8, 8)), ((4, 4, 4), (12, 12, 12))]):
+        k, j, i = np.meshgrid(*[np.arange(lo[d], hi[d] + 1) for d in (2, 1, 0)], indexing="ij")
+        want = np.stack([100.0 * q + i + 10.0 * j + 0.5 * k for q in range(3)])
+        assert np.array_equal(lev["data"], want)
