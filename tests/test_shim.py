@@ -57,3 +57,10 @@ def test_shim_writes_a_plotfile_without_a_gpu(tmp_path):
         k, j, i = np.meshgrid(*[np.arange(lo[d], hi[d] + 1) for d in (2, 1, 0)], indexing="ij")
         want = np.stack([100.0 * q + i + 10.0 * j + 0.5 * k for q in range(3)])
         assert np.array_equal(lev["data"], want)
+
+
+def test_shim_templates_instantiate():
+    """Every member of Operator::Elastic<T> and Solver::Nonlocal::Newton<T> compiles for the
+    isotropic, cubic and Laplacian models (explicit instantiation, compile only)."""
+    src = os.path.join(ROOT, "tests", "shim", "instantiate_all.cpp")
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), src], check=True)
