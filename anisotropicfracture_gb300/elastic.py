@@ -379,6 +379,30 @@ class Newton(Linear):
     def setNRIters(self, n):
         self.m_nriters = int(n)
 
+    @staticmethod
+    def Parse(value, pp):
+        """Newton<T>::Parse (src/Solver/Nonlocal/Newton.H:342-347): the Linear keys plus nriters."""
+        Linear.Parse(value, pp)
+        if "nriters" in pp:
+            value.setNRIters(int(pp["nriters"]))
+        return value
+
+    def compResidual(self, res, u, b, F0=None):
+        """Newton<T>::compResidual (src/Solver/Nonlocal/Newton.H:211-231): res = b - N(u) on every
+        level (device Fields, one per level; F0 per-level eigenstrains or None)."""
+        for lev in range(len(u)):
+            self.linop.NewtonResidual(lev, res[lev], u[lev], b[lev], None if F0 is None else F0[lev])
+
+    def W(self, w, u, F0=None):
+        """Newton<T>::W (src/Solver/Nonlocal/Newton.H:233-275): strain energy density per node."""
+        for lev in range(len(u)):
+            self.linop.NewtonDW(lev, u[lev], w=w[lev], F0=None if F0 is None else F0[lev])
+
+    def DW(self, dw, u, F0=None):
+        """Newton<T>::DW (src/Solver/Nonlocal/Newton.H:277-333): DW, 9 components row-major."""
+        for lev in range(len(u)):
+            self.linop.NewtonDW(lev, u[lev], dw=dw[lev], F0=None if F0 is None else F0[lev])
+
     def solve(self, u, b, model=None, tol_rel=None, tol_abs=None, F0=None):
         import torch
         u = u if isinstance(u, (list, tuple)) else [u]
