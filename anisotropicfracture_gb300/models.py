@@ -82,18 +82,27 @@ def cubic(C11, C12, C44, R):
     """Linear::Cubic::Define(C11, C12, C44, R): C'_pqst = R_pi R_qj R_sk R_tl C_ijkl stored in 21 slots
     (src/Model/Solid/Linear/Cubic.H:31-59).  R may be (3,3) or a stack (G,3,3); returns (21,) or (G,21).
     Each slot takes the value of the last (p,q,s,t), in loop order, that maps to it, as the reference's
-    assignment loop does."""
+    assignment loop does.  Each value is summed over (i,j,k,l) in the reference's loop order with the
+    reference's product order, so the result equals the reference's bit for bit."""
     R = np.asarray(R, dtype=np.float64)
     single = R.ndim == 2
     R = R.reshape(-1, 3, 3)
     C = cubic_tensor(C11, C12, C44)
-    full = np.einsum("gpi,gqj,gsk,gtl,ijkl->gpqst", R, R, R, R, C, optimize=True)
-    out = np.zeros((R.shape[0], 21))
+    last = {}
     for p in range(3):
         for q in range(3):
             for s in range(3):
                 for t in range(3):
-                    out[:, SLOT[p, q, s, t]] = full[:, p, q, s, t]
+                    last[int(SLOT[p, q, s, t])] = (p, q, s, t)
+    out = np.zeros((R.shape[0], 21))
+    for slot, (p, q, s, t) in last.items():
+        acc = np.zeros(R.shape[0])
+        for i in range(3):
+            for j in range(3):
+                for k in range(3):
+                    for l in range(3):
+                        acc = acc + R[:, p, i] * R[:, s, k] * C[i, j, k, l] * R[:, q, j] * R[:, t, l]
+        out[:, slot] = acc
     return out[0] if single else out
 
 

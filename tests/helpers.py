@@ -112,3 +112,43 @@ def golden_case(z, name):
     d = {k[len(p):]: z[k] for k in z.files if k.startswith(p)}
     d["C"] = golden_stiffness(d)
     return d
+
+
+# Per-node tolerance.  A node's error is measured against its own oracle value; nodes whose value
+# is below PERNODE_FLOOR x max|oracle| (values produced by cancellation of much larger stencil
+# terms, where a fused multiply-add on the GPU and a separate multiply and add in the oracle
+# round differently) are measured against that floor instead.
+PERNODE_FLOOR = 1e-3
+
+
+def pernode_err(a, ref, floor=PERNODE_FLOOR):
+    """max over nodes of |a - ref| / max(|ref_node|, floor * max|ref|)."""
+    s = float(np.abs(ref).max())
+    den = np.maximum(np.abs(ref), floor * (s if s > 0 else 1.0))
+    return float((np.abs(a - ref) / den).max())
+
+
+def pernode_report(a, ref):
+    """The worst per-node relative error at the floors 0, 1e-9, 1e-6, 1e-3 (x max|oracle|)."""
+    return {f: pernode_err(a, ref, f) for f in (0.0, 1e-9, 1e-6, 1e-3)}
+
+
+def golden_level(z, lname):
+    """The oracle level description stored as <lname>_level / <lname>_dxs in a fixture file."""
+    from oracle import pyoracle as po
+    v = [int(a) for a in z[lname + "_level"]]
+    L = po.Level()
+    for d in range(3):
+        L.dom_lo[d], L.dom_hi[d], L.lo[d], L.hi[d] = v[d], v[3 + d], v[6 + d], v[9 + d]
+        L.dx[d] = float(z[lname + "_dxs"][d])
+    L.ng = v[12]
+    return L
+
+
+def golden_prefixed(z, prefix):
+    """Entries of a fixture file whose key starts with `prefix`, without it, plus the rebuilt
+    per-node stiffness "C" when the entries describe one."""
+    d = {k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)}
+    if "C" in d or "tabs" in d:
+        d["C"] = golden_stiffness(d)
+    return d

@@ -1,14 +1,18 @@
 """GPU operator kernels vs the CPU oracle on the same seeded inputs, through the C ABI.
 
-Tolerance (FP64): every node within 1e-12 of the field's max-norm, i.e.
-max|gpu - oracle| <= 1e-12 * max|oracle| (the kernels fuse multiply-adds that the
-oracle keeps separate).  FP32 kernels: 2e-5 of the max-norm."""
+Tolerance (FP64), both required:
+- normwise: max|gpu - oracle| <= 1e-12 * max|oracle|;
+- per node: |gpu - oracle| <= 1e-12 * max(|oracle_node|, 1e-3 * max|oracle|), i.e. relative to the
+  node's own value wherever that is at least 1e-3 of the field's max-norm (helpers.pernode_err).
+The kernels fuse multiply-adds that the oracle keeps separate, so nodes whose value comes from
+cancelling much larger stencil terms differ in relative terms; the worst per-node error is printed
+at the floors 0, 1e-9, 1e-6 and 1e-3.  FP32 kernels: 2e-5 of the max-norm."""
 import numpy as np
 import pytest
 
 from anisotropicfracture_gb300 import models
 from anisotropicfracture_gb300.elastic import BCElastic, Elastic, Field, level_desc
-from helpers import bc_pull_z, bc_random, normwise_err, random_coeffs
+from helpers import bc_pull_z, bc_random, normwise_err, pernode_err, pernode_report, random_coeffs
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
@@ -54,7 +58,10 @@ def test_fapply_matches_oracle(model, cells, bckind, uniform):
     f = torch.zeros((3,) + L.shape, dtype=torch.float64, device="cuda")
     op.Fapply(0, 0, Field(f), Field(dev(u)))
     ref = po.fapply(L, model, Cf, bc.type, u, uniform)
-    assert normwise_err(host(f), ref) <= TOL64
+    got = host(f)
+    print("PERNODE fapply", model, cells, bckind, uniform, pernode_report(got, ref))
+    assert normwise_err(got, ref) <= TOL64
+    assert pernode_err(got, ref) <= TOL64
 
 
 @pytest.mark.parametrize("model", MODELS)
@@ -82,7 +89,10 @@ def test_diagonal_all_levels(model, bckind):
         Dg = torch.zeros((3,) + Lm.shape, dtype=torch.float64, device="cuda")
         op.Diagonal(0, m, Field(Dg))
         ref = po.diagonal(Lm, model, Cm, bc.type)
-        assert normwise_err(host(Dg), ref) <= TOL64, "mglev %d" % m
+        got = host(Dg)
+        print("PERNODE diagonal", model, bckind, m, pernode_report(got, ref))
+        assert normwise_err(got, ref) <= TOL64, "mglev %d" % m
+        assert pernode_err(got, ref) <= TOL64, "mglev %d" % m
         # coarse-level Fapply uses the restricted stiffness too
         u = rng.standard_normal((3,) + Lm.shape)
         f = torch.zeros_like(Dg)
@@ -100,7 +110,10 @@ def test_fsmooth_matches_oracle(model, nsweeps):
     op.Fsmooth(0, 0, Field(xd), Field(dev(b)), nsweeps, 2.0 / 3.0)
     Dg = po.diagonal(L, model, Cf, bc.type)
     ref = po.fsmooth(L, model, Cf, bc.type, Dg, x, b, nsweeps, 2.0 / 3.0)
-    assert normwise_err(host(xd), ref) <= TOL64
+    got = host(xd)
+    print("PERNODE fsmooth", model, nsweeps, pernode_report(got, ref))
+    assert normwise_err(got, ref) <= TOL64
+    assert pernode_err(got, ref) <= TOL64
 
 
 @pytest.mark.parametrize("model", MODELS)
@@ -111,7 +124,10 @@ def test_residual_and_norm(model):
     r = torch.zeros((3,) + L.shape, dtype=torch.float64, device="cuda")
     nrm = op.Residual(0, 0, Field(r), Field(dev(x)), Field(dev(b)))
     ref, rn = po.residual(L, model, Cf, bc.type, x, b)
-    assert normwise_err(host(r), ref) <= TOL64
+    got = host(r)
+    print("PERNODE residual", model, pernode_report(got, ref))
+    assert normwise_err(got, ref) <= TOL64
+    assert pernode_err(got, ref) <= TOL64
     assert abs(nrm - rn) <= TOL64 * rn
 
 
