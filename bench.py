@@ -51,8 +51,7 @@ JACOBI32_BYTES_PER_NODE_GRAINS = 12 + 12 + 12 + 2 + 12
 FAPPLY64_BYTES_PER_NODE_GRAINS = 24 + 2 + 24
 FAPPLY32_BYTES_PER_NODE_GRAINS = 12 + 2 + 12
 # measured DRAM bytes per node of the FP32 Jacobi sweep (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum at 193^3, larger than L2, mean of two launches;
-# profiles/jacobi32_dram_193cubed.md), keyed by grain map on/off
+# dram__bytes_write.sum at 193^3, larger than L2, mean of two launches), keyed by grain map on/off
 JACOBI32_TRAFFIC_PER_NODE = {True: 47.3, False: 131.1}
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
@@ -237,29 +236,259 @@ def cpu_single_thread(levels, bc, cpu):
                       "%d^3-node coarse level (%.2f s / %.3f s = %.1f)" % (nthreads, L["cells"] + 1, t1, tn, ratio)}
 
 
+def config1_solve_iters():
+    """(iterations of the two-level workload's FP64 solve, where that count comes from): the
+    oracle's own full solve (tests/golden/config1_oracle.npz, made by
+    tests/golden/make_config1_oracle.py) when its record is present."""
+    path = os.path.join(ROOT, "tests", "golden", "config1_oracle.npz")
+    if FP64_ITERS_OVERRIDE:
+        return FP64_ITERS_OVERRIDE, "AE_FP64_ITERS"
+    if os.path.exists(path):
+        z = np.load(path)
+        return int(z["iters"]), "the oracle's full FP64 solve of this workload (%.0f s on %d host threads)" % (
+            float(z["seconds"]), int(z["threads"]))
+    return 167, "the GPU FP64 solve of this workload"
+
+
+def config_of(n):
+    """The config both arms print (identical dicts; the precision each arm computes in is a
+    top-level key)."""
+    return {"workload": workload_label(n), "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, CG bottom",
+            "tol_rel": 1e-8, "nodes": 2 * (n + 1) ** 3}
+
+
 def run_reference(args, rank):
-    """Reference arm: the reference's CPU path (its C++ restatement in oracle/, the reference
-    itself needs AMReX/Eigen/MPI, absent here) timed on the host cores."""
+    """Reference arm: the reference's CPU path (its C++ restatement in oracle/, pinned bit for bit
+    to the reference's own compiled per-node code; the reference as a whole needs AMReX, Eigen and
+    MPI, absent here) on the host cores.  The set-up (stiffness restricted to every multigrid
+    level, diagonals) is timed once; each step then runs set-up plus --ref-sample-iters composite
+    iterations, and the solve time is extrapolated to the iteration count of a full solve."""
     if rank != 0:
         return
+    from oracle import pyoracle as po
+    po.set_threads(os.cpu_count())
     levels, bc = workload(args.cells)
-    iters = FP64_ITERS_OVERRIDE or args.ref_iters
-    rhs = [oracle_rhs(L, bc) for L in levels]
-    samples = []
+    iters, src = config1_solve_iters()
+    Ls = [oracle_level(L) for L in levels]
+    Cs = [L["C"] for L in levels]
+    bs = [oracle_rhs(L, bc) for L in levels]
+    us = [np.zeros_like(b) for b in bs]
+    kw = dict(max_fmg_iter=0, bottom=0, nu1=1, nu2=1)
+    t0 = time.perf_counter()
+    po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, us, bs, 1e-30, 0.0, max_iter=0, **kw)
+    t_setup = time.perf_counter() - t0
+    m = max(1, args.ref_sample_iters)
+    steps = []
     for k in range(args.warmup + args.steps):
-        cb = cpu_oracle_sample(levels, bc, iters, sample_iters=1, rhs=rhs)
+        it = 1 if k < args.warmup else m
+        t0 = time.perf_counter()
+        po.solve_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, us, bs, 1e-30, 0.0, max_iter=it, **kw)
         if k >= args.warmup:
-            samples.append(1.0 / cb["value"])
-    t = float(np.mean(samples))
-    v = 1.0 / t
+            steps.append(time.perf_counter() - t0)
+    t_step = float(np.mean(steps))
+    t_iter = max(t_step - t_setup, 1e-9) / m
+    t_solve = t_setup + iters * t_iter
+    v = 1.0 / t_solve
+    cores = po.lib().orc_num_threads()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_label(args.cells),
-                       "precision": "fp64", "cycle": "V(2,2) Jacobi, CG bottom", "tol_rel": 1e-8},
-            "cpu_baseline": dict(cb, value=v),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "precision": "fp64", "data": "synthetic",
+            "config": config_of(args.cells),
+            "solve_seconds_extrapolated": t_solve,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "FP64 oracle on the full two-level 257^3 workload, %d threads: each step = "
+                                       "set-up + %d composite iterations (%.1f s); set-up %.1f s, %.2f s per "
+                                       "iteration; one solve = set-up + %d iterations (from %s) = %.0f s"
+                                       % (cores, m, t_step, t_setup, t_iter, iters, src, t_solve)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def pull_z_bc(uz):
+    """u = 0 on z = 0, u_z = uz (u_x = u_y = 0) on z = 1, traction-free lateral faces; edges and
+    corners touching z = 0 / z = 1 take the z-face type."""
+    from anisotropicfracture_gb300.elastic import BCElastic, FACES
+    bc = BCElastic()
+    for f in FACES:
+        for d in range(3):
+            bc.Set(f, d, bc.Displacement, 0.0)
+    for f in ["XLO", "XHI", "YLO", "YHI", "XLO_YLO", "XLO_YHI", "XHI_YLO", "XHI_YHI"]:
+        for d in range(3):
+            bc.Set(f, d, bc.Traction, 0.0)
+    for f in FACES:
+        if "ZHI" in f:
+            bc.Set(f, 2, bc.Displacement, uz)
+    return bc
+
+
+def pernode_err(a, ref, floor=1e-3):
+    """max over nodes of |a - ref| / max(|ref_node|, floor * max|ref|)"""
+    s = float(np.abs(ref).max())
+    return float((np.abs(a - ref) / np.maximum(np.abs(ref), floor * (s if s > 0 else 1.0))).max())
+
+
+def normwise(a, ref):
+    s = float(np.abs(ref).max())
+    return float(np.abs(a - ref).max() / (s if s > 0 else 1.0))
+
+
+# ---------------------------------------------------------------- the 64^3 single-level workload
+def bench_config0(args):
+    """64^3 cells (65^3 nodes), isotropic sphere inclusion (E 10 / 1, nu 0.3, 2-cell diffuse
+    interface), pulled along z, V(2,2) + CG to 1e-8: GPU FP64 and mixed solves/s (device time over
+    several solves, and end to end through host buffers), against the oracle's full FP64 solve on
+    the host cores, timed in full: its iterations, the displacement error of each GPU solution
+    against it, and the oracle's residual of each GPU solution."""
+    import torch
+    from anisotropicfracture_gb300 import microstructure, models
+    from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
+    from oracle import pyoracle as po
+    n = 64
+    Cf = microstructure.sphere_inclusion_iso((0, 0, 0), (n, n, n), (1.0 / n,) * 3)
+    bc = pull_z_bc(0.01)
+    L = po.level(n)
+    b = po.bc_init(L, bc.type, bc.val, np.zeros((3,) + L.shape))
+    op = Elastic([level_desc(n)], models.ISOTROPIC)
+    op.SetModel(0, Field(Cf))
+    op.SetBC(bc)
+    op.SetUniform(False)
+    op.prepareForSolve()
+    stream = torch.cuda.Stream()
+    op.set_stream(stream.cuda_stream)
+    s = Linear(op)
+    s.setMaxFmgIter(0)
+    s.setBottomSolver("cg")
+    s.setPreSmooth(1)
+    s.setPostSmooth(1)
+    s.opts.max_iter = 400
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros_like(bd)
+    bh = torch.from_numpy(b).pin_memory()
+    xh = torch.zeros_like(bh).pin_memory()
+    reps = max(1, args.config0_reps)
+    out = {"workload": "64^3 cells (65^3 nodes), isotropic sphere inclusion r 0.25 (E 10 / 1, nu 0.3, 2-cell diffuse "
+                       "interface), u_z = 0.01 on z = 1, traction-free sides, V(2,2) Jacobi + CG, tol_rel 1e-8",
+           "unit": UNIT, "l2": "resident in L2 (17.6 MB per FP64 apply): reported in solves/s, not as HBM fraction"}
+    xs = {}
+    for prec, inner in (("fp64", 1), ("mixed", args.config0_inner)):
+        s.setPrecision(prec)
+        s.opts.inner_cycles = inner
+
+        def one():
+            with torch.cuda.stream(stream):
+                xd.zero_()
+            s.solve(Field(xd), Field(bd), 1e-8, 0.0)
+
+        for _ in range(2):
+            one()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            one()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        xs[prec] = xd.cpu().numpy()
+        st = s.stats
+        rec = {"value": 1000.0 / ms, "ms_per_solve": ms, "iters": st.iters, "cycles": st.cycles,
+               "inner_cycles": inner, "converged": bool(st.converged), "resfinal": st.resfinal, "target": st.target}
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            xh.zero_()
+            s.solve(Field(xh.numpy()), Field(bh.numpy()), 1e-8, 0.0)
+        e2e = (time.perf_counter() - t0) / reps
+        rec["e2e"] = {"value": 1.0 / e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * b.nbytes,
+                      "d2h_bytes_per_step": b.nbytes}
+        out[prec] = rec
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    op.close()
+    if not args.no_cpu:
+        po.set_threads(os.cpu_count())
+        t0 = time.perf_counter()
+        ref, st, rc = po.solve(L, po.ORC_ISOTROPIC, Cf, bc.type, np.zeros_like(b), b, 1e-8, 0.0, max_fmg_iter=0,
+                               bottom=0, nu1=1, nu2=1, max_iter=400)
+        t_cpu = time.perf_counter() - t0
+        bn = float(np.abs(b).max())
+        out["oracle"] = {"iters": st.iters, "converged": bool(rc == 0 and st.converged), "seconds": t_cpu,
+                         "threads": po.lib().orc_num_threads()}
+        for prec in ("fp64", "mixed"):
+            _, rn = po.residual(L, po.ORC_ISOTROPIC, Cf, bc.type, xs[prec], b)
+            out[prec]["displacement_err_vs_oracle"] = normwise(xs[prec], ref)
+            out[prec]["oracle_rel_residual"] = rn / bn
+        out["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": po.lib().orc_num_threads(),
+                               "kind": "port", "sample": "the oracle's full FP64 solve (%d V-cycles), timed in full"
+                                                         % st.iters}
+    return out
+
+
+def oracle_check(levels, bc, rhs, sols):
+    """The oracle on the GPU's final solutions of the two-level workload: its composite residual
+    ||b - A x||_inf / ||b||_inf (MLMG's computeMLResidual restated), and, when the committed record
+    of the oracle's own full solve (tests/golden/config1_oracle.npz) is present, the displacement
+    error at its subsampled nodes, relative to the max-norm of the oracle's solution there."""
+    from oracle import pyoracle as po
+    Ls = [oracle_level(L) for L in levels]
+    Cs = [L["C"] for L in levels]
+    bn = max(float(np.abs(valid_part(L, b)).max()) for L, b in zip(levels, rhs))
+    out = {"residual": "oracle composite ||b - A x||_inf / ||b||_inf of each GPU solution (solve target 1e-8)"}
+    for name, xs in sols.items():
+        t0 = time.perf_counter()
+        rn = po.residual_amr(Ls, po.ORC_MAJORMINOR, Cs, bc.type, xs, rhs)
+        out[name] = {"oracle_rel_residual": rn / bn, "seconds": time.perf_counter() - t0}
+    path = os.path.join(ROOT, "tests", "golden", "config1_oracle.npz")
+    if os.path.exists(path):
+        z = np.load(path)
+        k = int(z["stride"])
+        subs = [z["sub%d" % a] for a in range(len(levels))]
+        scale = max(float(np.abs(v).max()) for v in subs)
+        out["cpu_oracle_solve"] = {"iters": int(z["iters"]), "seconds": float(z["seconds"]),
+                                   "threads": int(z["threads"]), "resfinal": float(z["resfinal"]),
+                                   "compared": "every %d-th node of each level's valid box (%d nodes)"
+                                               % (k, sum(v[0].size for v in subs))}
+        for name, xs in sols.items():
+            err = max(float(np.abs(valid_part(L, x)[:, ::k, ::k, ::k] - v).max())
+                      for L, x, v in zip(levels, xs, subs))
+            out[name]["displacement_err_vs_cpu_oracle_solve"] = err / scale
+    return out
+
+
+def parity_at_size(op, levels, bc, device):
+    """One FP64 Fapply, residual and Fsmooth (two sweeps) of the GPU on each full-size level,
+    against the oracle on the same seeded inputs: normwise error and the worst per-node relative
+    error (floor 1e-3 of the field's max-norm)."""
+    import torch
+    from anisotropicfracture_gb300.elastic import Field
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(11)
+    out = {"tolerance": "1e-12 normwise and per node (floor 1e-3 of the max-norm)"}
+    for a, L in enumerate(levels):
+        Lo = oracle_level(L)
+        lo = tuple(L["store_lo"])
+        shape = (3,) + level_shape(L)
+        u = rng.standard_normal(shape)
+        b = rng.standard_normal(shape)
+        ud, bd = torch.from_numpy(u).to(device), torch.from_numpy(b).to(device)
+        f = torch.zeros_like(ud)
+        op.Fapply(a, 0, Field(f, lo), Field(ud, lo))
+        r = torch.zeros_like(ud)
+        op.Residual(a, 0, Field(r, lo), Field(ud, lo), Field(bd, lo))
+        xd = ud.clone()
+        op.Fsmooth(a, 0, Field(xd, lo), Field(bd, lo), 2, 2.0 / 3.0)
+        torch.cuda.synchronize()
+        got = {"fapply": f.cpu().numpy(), "residual": r.cpu().numpy(), "fsmooth": xd.cpu().numpy()}
+        del ud, bd, f, r, xd
+        t0 = time.perf_counter()
+        ref = {"fapply": po.fapply(Lo, po.ORC_MAJORMINOR, L["C"], bc.type, u),
+               "residual": po.residual(Lo, po.ORC_MAJORMINOR, L["C"], bc.type, u, b)[0]}
+        D = po.diagonal(Lo, po.ORC_MAJORMINOR, L["C"], bc.type)
+        ref["fsmooth"] = po.fsmooth(Lo, po.ORC_MAJORMINOR, L["C"], bc.type, D, u, b, 2, 2.0 / 3.0)
+        rec = {"nodes": int(np.prod(shape[1:])), "oracle_seconds": time.perf_counter() - t0}
+        for k in got:
+            g, e = valid_part(L, got[k]), valid_part(L, ref[k])
+            rec[k] = {"normwise": normwise(g, e), "per_node": pernode_err(g, e)}
+        out["level%d" % a] = rec
+    return out
 
 
 # ---------------------------------------------------------------- damaged polycrystal, 193^3 nodes
@@ -340,6 +569,11 @@ def bench_damaged_polycrystal(args):
                                    "cores": po.lib().orc_num_threads(), "kind": "port",
                                    "sample": "FP64 oracle, set-up %.1f s + 1 V-cycle at %.2f s, extrapolated to the "
                                              "%d cycles of the FP64 solve" % (t_setup, t_iter, iters)}
+            if not args.no_parity:  # the oracle's residual of each GPU solution
+                bn = float(np.abs(bh).max())
+                for prec in ("fp64", "mixed"):
+                    _, rn = po.residual(L, po.ORC_MAJORMINOR, C, bc.type, xs[prec], bh)
+                    out[prec]["oracle_rel_residual"] = rn / bn
         except Exception as e:  # pragma: no cover
             out["cpu_baseline"] = {"value": None, "sample": "failed: %s" % e}
     del C
@@ -525,6 +759,29 @@ def bench_batch(args, lib, rank=0, world=1):
                                              "scaled per node to the mean cell" % (ns, nn, secs)}
         except Exception as e:  # pragma: no cover
             out["cpu_baseline"] = {"value": None, "sample": "failed: %s" % e}
+        if not args.no_parity:
+            out["oracle_check"] = cells_oracle_check(work, sols, max(1, args.batch_cpu_sample))
+    return out
+
+
+def cells_oracle_check(work, sols, nsample):
+    """The oracle's mean-free residual ||b - A w - c||_inf / ||b||_inf of the GPU's batched
+    solutions (mixed and FP64) for the first `nsample` cells."""
+    from anisotropicfracture_gb300 import cells, models
+    from oracle import pyoracle as po
+    out = {"cells": nsample, "what": "oracle mean-free residual / ||b||_inf of the batched GPU solutions"}
+    worst = {k: 0.0 for k in sols}
+    for c, w in enumerate(work[:nsample]):
+        n = w["n"]
+        L = po.rve_level(n)
+        Cf = cells.rve_stiffness(n, w["seeds"], w["table"])
+        b = po.rve_rhs(L, models.MAJORMINOR, Cf, _exx())
+        bn = float(np.abs(b).max())
+        for k, ws in sols.items():
+            _, _, rn = po.rve_residual(L, models.MAJORMINOR, Cf, np.ascontiguousarray(ws[c]), b)
+            worst[k] = max(worst[k], rn / bn)
+    for k in sols:
+        out[k + "_worst_rel_residual"] = worst[k]
     return out
 
 
@@ -552,30 +809,60 @@ def serve_run(work, rate, precision, inner, seed=7):
     st = S.stats()
     S.close()
     lat = np.array([r["latency"] for r in res])
+    queue = np.array([r["t_admit"] - r["t_submit"] for r in res])
+    service = np.array([r["t_done"] - r["t_admit"] for r in res])
     good = [r for r in res if r["status"] == 0]
     first = min(r["t_submit"] for r in res)
     last = max(r["t_done"] for r in res)
     nsolves = sum(len(r["stats"]) for r in good)
-    return {"rate": rate, "requests": len(work), "ok": len(good) == len(res), "p50_s": float(np.percentile(lat, 50)),
-            "p99_s": float(np.percentile(lat, 99)), "solves_per_s": nsolves / (last - first),
-            "iterations": st["iterations"], "busy_s": st["busy_seconds"]}
+    # requests resident on the device (admitted, not yet done) over time: time-weighted mean, max
+    ev = sorted([(r["t_admit"], 1) for r in res] + [(r["t_done"], -1) for r in res])
+    live, peak, area, t_prev = 0, 0, 0.0, ev[0][0]
+    for t, d in ev:
+        area += live * (t - t_prev)
+        live += d
+        peak = max(peak, live)
+        t_prev = t
+    span = max(ev[-1][0] - ev[0][0], 1e-9)
+
+    def pct(a, q):
+        return float(np.percentile(a, q))
+
+    return {"rate": rate, "requests": len(work), "ok": len(good) == len(res),
+            "offered_solves_per_s": rate * len(cells.unit_strains()),
+            "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+            "queue_p50_s": pct(queue, 50), "queue_p99_s": pct(queue, 99),
+            "service_p50_s": pct(service, 50), "service_p99_s": pct(service, 99),
+            "resident_mean": area / span, "resident_max": peak,
+            "solves_per_s": nsolves / (last - first), "iterations": st["iterations"], "busy_s": st["busy_seconds"]}
 
 
 def bench_serve(args):
+    """Served cells: for each arrival rate a fresh server takes a Poisson stream of requests.
+    Latency (submission to result) is split into queueing delay (submission to admission) and
+    service time (admission to result); `resident_*` counts requests on the device at once.
+    The sub-capacity rates show overlap below saturation; above capacity the queue grows and
+    latency measures the backlog."""
     rates = [float(r) for r in args.serve_rates.split(",") if r]
-    work = serve_workload(args.serve_requests)
+    rates64 = [float(r) for r in args.serve_fp64_rates.split(",") if r]
+    work = serve_workload(max(args.serve_requests, args.serve_fp64_requests))
     out = {"workload": "Poisson streams (seed 6) of periodic polycrystal cells, edges uniform in {32..128 step 8}, "
                        "8-64 grains, 6 unit strains (1e-3) per request, tol_rel 1e-8",
-           "requests_per_rate": len(work), "mean_nodes": float(np.mean([w["n"] ** 3 for w in work])),
+           "requests_per_rate": {"mixed": args.serve_requests, "fp64": args.serve_fp64_requests},
+           "mean_nodes": float(np.mean([w["n"] ** 3 for w in work[:args.serve_requests]])),
            "inner_cycles": args.batch_inner, "unit": UNIT}
     # warm-up: one small request (library load, first graph capture)
     serve_run(work[:1], 1000.0, 1, args.batch_inner)
-    for prec, name in ((1, "mixed"), (0, "fp64")):
-        runs = [serve_run(work, r, prec, args.batch_inner) for r in rates]
-        out[name] = runs
-    peak_m = max(r["solves_per_s"] for r in out["mixed"])
-    peak_f = max(r["solves_per_s"] for r in out["fp64"])
-    out["mixed_over_fp64"] = peak_m / peak_f
+    out["mixed"] = [serve_run(work[:args.serve_requests], r, 1, args.batch_inner) for r in rates]
+    out["fp64"] = [serve_run(work[:args.serve_fp64_requests], r, 0, args.batch_inner) for r in rates64]
+    cap_m = max(r["solves_per_s"] for r in out["mixed"])
+    cap_f = max(r["solves_per_s"] for r in out["fp64"])
+    out["capacity_solves_per_s"] = {"mixed": cap_m, "fp64": cap_f,
+                                    "how": "highest delivered solves/s over the arrival rates"}
+    for name, cap in (("mixed", cap_m), ("fp64", cap_f)):
+        for r in out[name]:
+            r["load"] = r["offered_solves_per_s"] / cap
+    out["mixed_over_fp64"] = cap_m / cap_f
     return out
 
 
@@ -594,10 +881,14 @@ def main():
     ap.add_argument("--mixed-tight-tol", type=float, default=0.0,
                     help="also time the mixed solve to this residual and report its error (0: off)")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    # composite FP64 iterations of the two-level 257^3 polycrystal solve: measured by this benchmark's FP64 solve
-    # (167), which follows the oracle iteration for iteration
-    ap.add_argument("--ref-iters", type=int, default=167)
+    ap.add_argument("--ref-sample-iters", type=int, default=3,
+                    help="composite oracle iterations per step of the reference arm")
     ap.add_argument("--cpu-sample-iters", type=int, default=1)
+    ap.add_argument("--no-config0", action="store_true", help="skip the 64^3 single-level workload")
+    ap.add_argument("--config0-reps", type=int, default=5)
+    ap.add_argument("--config0-inner", type=int, default=4, help="FP32 cycles per FP64 residual, 64^3 workload")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size operator comparison and the oracle residuals of the GPU solutions")
     ap.add_argument("--no-cpu", action="store_true")
     # 12: an FP64 composite residual costs about one FP32 V-cycle here, and a solve overshoots its
     # cycle count by (inner - 1) / 2 cycles on average; 8 / 12 / 16 gave 0.413 / 0.430 / 0.419
@@ -621,8 +912,11 @@ def main():
                     help="FP32 cycles per FP64 residual for the batched and served cells")
     ap.add_argument("--batch-single-limit", type=int, default=0, help="cells timed one at a time (0: all)")
     ap.add_argument("--batch-cpu-sample", type=int, default=4)
-    ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-rates", default="50,200,2000")
+    ap.add_argument("--serve-requests", type=int, default=200, help="requests per arrival rate, mixed precision")
+    ap.add_argument("--serve-rates", default="4,50,100,200,500,1000,2000",
+                    help="arrival rates (requests/s), mixed precision")
+    ap.add_argument("--serve-fp64-requests", type=int, default=40, help="requests per arrival rate, FP64")
+    ap.add_argument("--serve-fp64-rates", default="1,50", help="arrival rates (requests/s), FP64")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -846,6 +1140,15 @@ def main():
     h2d = sum(b.numel() * 8 for b in rhs_p) * 2  # rhs and initial guess
     d2h = sum(b.numel() * 8 for b in sol_p)
 
+    # the oracle on the GPU's solutions, and the FP64 operators at full size against the oracle
+    checks, parity = None, None
+    if rank == 0 and not args.no_cpu and not args.no_parity:
+        sols = {"mixed": x_mixed}
+        if args.fp64_steps > 0:
+            sols["fp64"] = x64
+        checks = oracle_check(levels, bc, rhs_h, sols)
+        parity = parity_at_size(op, levels, bc, dev)
+
     # roofline of the dominant kernel: FP32 fused Jacobi sweep on the finest coarse level
     ms_jac = C.c_double(0.0)
     _lib.check(lib.ae_profile_kernel(op.handle, 1, 0, 0, 1, 20, C.byref(ms_jac)))
@@ -869,7 +1172,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
-            cpu = cpu_oracle_sample(levels, bc, fp64_iters or iters_mixed, sample_iters=args.cpu_sample_iters,
+            cpu = cpu_oracle_sample(levels, bc, config1_solve_iters()[0], sample_iters=args.cpu_sample_iters,
                                     rhs=rhs_h)
             cpu["single_thread"] = cpu_single_thread(levels, bc, cpu)
         except Exception as e:  # pragma: no cover
@@ -880,14 +1183,13 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": workload_label(args.cells),
-                   "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, CG bottom", "tol_rel": 1e-8,
-                   "precision": "mixed: FP32 cycle in FP64 refinement", "inner_cycles": args.inner,
-                   "stiffness": ("per-node coefficients (ae_op_set_model)" if args.per_node_model else
-                                 "Voronoi grain ids + per-grain table (ae_op_set_model_grains)"),
-                   "nodes": nodes,
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (stiffness %.1f GB)" % (sum(L["C"].nbytes for L in levels) / 1e9)},
+        "precision": "mixed: FP32 cycle in FP64 refinement",
+        "config": config_of(args.cells),
+        "run": {"inner_cycles": args.inner,
+                "stiffness": ("per-node coefficients (ae_op_set_model)" if args.per_node_model else
+                              "Voronoi grain ids + per-grain table (ae_op_set_model_grains)"),
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "l2": "inputs larger than L2 (stiffness %.1f GB)" % (sum(L["C"].nbytes for L in levels) / 1e9)},
         "iters_mixed": res_mixed[0], "resfinal_mixed": res_mixed[1], "target": res_mixed[2],
         "converged": bool(res_mixed[3]),
         "fp64": {"value": (world * 1000.0 / ms_fp64) if ms_fp64 else None, "unit": UNIT,
@@ -895,6 +1197,8 @@ def main():
         "mixed_over_fp64": (ms_fp64 / ms_mixed) if ms_fp64 else None,
         "displacement_err_mixed_vs_fp64": disp_err,
         "fp64_oracle": oracle,
+        "oracle_check": checks,
+        "parity_at_size": parity,
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "FP32 fused Jacobi sweep (cubic), coarse level 257^3",
                      "achieved": jac_gbs, "peak": peak, "unit": "GB/s", "frac": jac_gbs / peak,
@@ -914,6 +1218,11 @@ def main():
         "cpu_baseline": cpu,
     }
     op.close()
+    if rank == 0 and not args.no_config0:
+        try:
+            line["config0"] = bench_config0(args)
+        except Exception as e:  # pragma: no cover
+            line["config0"] = {"error": str(e)}
     add_cell_workloads(args, lib, line, rank, world)
     if rank == 0:
         print(json.dumps(line), flush=True)

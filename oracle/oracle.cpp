@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -985,6 +986,43 @@ int orc_num_mg_levels(const orc_level* L, int max_mg_levels) {
         ++n;
     }
     return n;
+}
+
+// MLMG::computeMLResidual restated on its own (the composite residual Amr::ml_residual takes, with
+// no multigrid set-up): r_a = b_a - A_a u_a on every AMR level, finest first, and on each coarser
+// level the fine residual restricted onto the nodes the finer patch covers (reflux,
+// src/Operator/Operator.cpp:728-839).  rs may be NULL (scratch is allocated); norm_inf gets the
+// max-norm over the valid nodes of every level.
+int orc_residual_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
+                     int uniform, const double* const* us, const double* const* bs, double* const* rs,
+                     double* norm_inf) {
+    if (namr < 1 || Ls[0].ng != 0) return -1;
+    std::vector<std::unique_ptr<Lev>> L;
+    std::vector<std::vector<double>> own(namr);
+    std::vector<double*> r(namr);
+    for (int a = 0; a < namr; ++a) {
+        L.emplace_back(new Lev(Ls[a]));
+        if (rs && rs[a]) {
+            r[a] = rs[a];
+        } else {
+            own[a].assign(3 * L[a]->nn, 0.0);
+            r[a] = own[a].data();
+        }
+    }
+    for (int a = namr - 1; a >= 0; --a) {
+        residual(*L[a], model, Cs[a], bctype, uniform, us[a], bs[a], r[a]);
+        if (a + 1 < namr) restrict_box(*L[a], *L[a + 1], 3, r[a], r[a + 1], isect(covered_by(*L[a + 1]), L[a]->dom));
+    }
+    double m = 0.0;
+    for (int a = 0; a < namr; ++a) {
+        const Box v = isect(L[a]->valid, L[a]->dom);
+        for (int n = 0; n < 3; ++n)
+            for (int k = v.lo[2]; k <= v.hi[2]; ++k)
+                for (int j = v.lo[1]; j <= v.hi[1]; ++j)
+                    for (int i = v.lo[0]; i <= v.hi[0]; ++i) m = amax(m, r[a][n * L[a]->nn + L[a]->at(i, j, k)]);
+    }
+    if (norm_inf) *norm_inf = m;
+    return 0;
 }
 
 // MLMG::solve restated: convergence when the composite ||r||_inf <= max(tol_abs, tol_rel * max_norm),

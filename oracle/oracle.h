@@ -97,6 +97,11 @@ int orc_solve(const orc_level* L, int model, const double* C, const int* bctype,
 int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
                   double* const* us, const double* const* bs, double tol_rel, double tol_abs,
                   const orc_opts* opts, orc_stats* stats);
+/* composite residual of given solutions (MLMG::computeMLResidual: per-level b - A u, the fine
+ * residual restricted onto covered coarse nodes); rs (one field per level) may be NULL */
+int orc_residual_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
+                     int uniform, const double* const* us, const double* const* bs, double* const* rs,
+                     double* norm_inf);
 /* number of multigrid levels the solver builds for this level */
 int orc_num_mg_levels(const orc_level* L, int max_mg_levels);
 

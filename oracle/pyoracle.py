@@ -245,6 +245,32 @@ def solve_amr(Ls, model, Cs, bctype, us, bs, tol_rel=1e-8, tol_abs=0.0, **kw):
     return us, st, rc
 
 
+def residual_amr(Ls, model, Cs, bctype, us, bs, uniform=False, want_fields=False):
+    """Composite residual max-norm of the solutions `us` (MLMG::computeMLResidual restated:
+    per-level b - A u, reflux of each finer level's residual onto the coarse nodes it covers).
+    Returns the norm, or (norm, per-level residual fields) with want_fields."""
+    n = len(Ls)
+    f = lib().orc_residual_amr
+    f.argtypes = [C.POINTER(Level), C.c_int, C.c_int, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int),
+                  C.c_int, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double)),
+                  C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_double)]
+    La = (Level * n)(*Ls)
+    Cs = [np.ascontiguousarray(c, dtype=np.float64) for c in Cs]
+    us = [np.ascontiguousarray(u, dtype=np.float64) for u in us]
+    bs = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+    rs = [np.zeros_like(u) for u in us] if want_fields else None
+    Cp = (C.POINTER(C.c_double) * n)(*[_d(c) for c in Cs])
+    up = (C.POINTER(C.c_double) * n)(*[_d(u) for u in us])
+    bp = (C.POINTER(C.c_double) * n)(*[_d(b) for b in bs])
+    rp = (C.POINTER(C.c_double) * n)(*[_d(r) for r in rs]) if want_fields else None
+    bt, btp = _i(bctype)
+    nrm = C.c_double(0.0)
+    rc = f(La, n, model, Cp, btp, int(uniform), up, bp, rp, C.byref(nrm))
+    if rc != 0:
+        raise RuntimeError("orc_residual_amr failed: %d" % rc)
+    return (nrm.value, rs) if want_fields else nrm.value
+
+
 def amr_levels(n, nlev, shrink=4):
     """Levels of the reference's test hierarchy (src/Test/Operator/Elastic.cpp:59-92): level 0
     n^3 cells on the unit cube; each finer level refines the central half of the previous one."""
