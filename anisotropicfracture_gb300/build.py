@@ -16,7 +16,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", CSRC, "-I", INCLUDE]
 
-SOURCES = ["ae_kernels_f64.cu", "ae_kernels_f32.cu", "ae_api.cu", "ae_noalloc.cu", "ae_cells_kernels.cu",
+SOURCES = ["ae_kernels_f64.cu", "ae_kernels_f32.cu", "ae_split.cu", "ae_api.cu", "ae_noalloc.cu", "ae_cells_kernels.cu",
            "ae_cells.cu", "ae_server.cu", "ae_plotfile.cpp"]
 
 

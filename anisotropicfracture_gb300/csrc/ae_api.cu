@@ -26,6 +26,7 @@
 
 #include "../../include/aefast.h"
 #include "ae_launch.h"
+#include "ae_split.h"
 
 #define AE_CHECK(x)                                                                              \
     do {                                                                                         \
@@ -94,6 +95,10 @@ struct MGLevel {
     float* gtab32 = nullptr;
     int ngrains = 0, gcap = 0;
     bool grains = false;
+    // FP32 sweeps of a grain-map level split into a tiled interior kernel and a node list
+    // (ae_split.cu); built by prepare32, rebuilt after the model changes
+    SplitList split;
+    bool split_built = false;
     // coarsest MG level of AMR level 0: its operator as an FP64 CSR matrix, for the bottom solve
     // of the FP32 cycle (assembled by prepare32)
     int* csr_rowptr = nullptr;
@@ -134,6 +139,7 @@ struct ae_op_s {
     bool have32 = false;
     bool prepared32 = false;
     bool tiled32 = false, tiled64 = false;  // z-marching tiled sweeps per precision (opt-in)
+    bool split32 = true;                    // split FP32 sweeps on grain-map levels (AE_SPLIT=0: off)
     long long bytes = 0;
     std::vector<void*> allocs;
     void* stage = nullptr;  // device staging for host fabs
@@ -153,6 +159,11 @@ struct ae_op_s {
         return static_cast<T*>(p);
     }
     ~ae_op_s() {
+        for (auto& A : amr)
+            for (auto& L : A.mg) {
+                if (L.split.list) cudaFree(L.split.list);
+                if (L.split.gidm) cudaFree(L.split.gidm);
+            }
         for (void* p : allocs) cudaFree(p);
         if (stage) cudaFree(stage);
         if (stage2) cudaFree(stage2);
@@ -169,6 +180,15 @@ struct ae_op_s {
         P.model = model;
         P.uniform = uniform;
         return P;
+    }
+    // the grain-map level whose FP32 stiffness is C, when its sweeps are split; else nullptr
+    const MGLevel* split_for(const float* C) const {
+        if (!split32) return nullptr;
+        for (const AmrLevel& A : amr) {
+            const MGLevel& L = A.mg[0];
+            if (L.grains && L.split_built && C == L.C32) return &L;
+        }
+        return nullptr;
     }
     // the grain tables of the level whose stiffness array is C, if it has them
     template <class R>
@@ -229,6 +249,7 @@ Geo coarsen_geo(const Geo& g) {
         c.dx[d] = g.dx[d] * 2.0;
     }
     c.ng = 0;
+    c.px = 0;
     return c;
 }
 
@@ -380,7 +401,30 @@ void prepare32(ae_op* op) {
         }
     AE_CHECK(cudaStreamSynchronize(op->st));
     assemble_bottom(op);
+    // node lists and id/mask arrays of the split FP32 sweeps on grain-map levels
+    if (op->split32)
+        for (auto& A : op->amr) {
+            MGLevel& L = A.mg[0];
+            if (!L.grains || L.split_built || (L.g.ng != 0 && L.g.ng < 2) || L.ngrains > kSplitMaxGrains ||
+                !split_supported(L.g))
+                continue;
+            split_build(L.g, cview(level_view(L.g, L.gid)), L.split, op->st, op->dnorm + 7);
+            if (const char* e = std::getenv("AE_SPLIT_KZ")) L.split.kz = std::atoi(e);
+            L.split_built = true;
+        }
     op->prepared32 = true;
+}
+
+// dflag[2] is set by the split sweep's tiled kernel when a TMA load did not complete within its
+// wait limit; the sweep's output is then incomplete
+void check_tma_flag(ae_op* op) {
+    int f = 0;
+    AE_CHECK(cudaMemcpyAsync(&f, op->dflag + 2, sizeof(int), cudaMemcpyDeviceToHost, op->st));
+    AE_CHECK(cudaStreamSynchronize(op->st));
+    if (f) {
+        AE_CHECK(cudaMemsetAsync(op->dflag + 2, 0, sizeof(int), op->st));
+        throw ApiErr(AE_ERR_CUDA, "a shared-memory tile load of the split FP32 sweep did not complete");
+    }
 }
 
 double read_norm(ae_op* op, int slot) {
@@ -408,6 +452,13 @@ void prepare(ae_op* op) {
             launch_diagonal<double>(op->params(L.g), cview(level_view(L.g, L.C)), level_view(L.g, L.D),
                                     level_view(L.g, L.invD), op->dflag, st);
     op->prepared32 = false;
+    for (auto& A : op->amr)
+        for (auto& L : A.mg) {
+            if (L.split.list) AE_CHECK(cudaFree(L.split.list));
+            if (L.split.gidm) AE_CHECK(cudaFree(L.split.gidm));
+            L.split = SplitList{};
+            L.split_built = false;
+        }
     int flag = 0;
     AE_CHECK(cudaMemcpyAsync(&flag, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
     AE_CHECK(cudaStreamSynchronize(st));
@@ -434,6 +485,14 @@ void sweep_jacobi(ae_op* op, const Geo& g, const R* C, const R* invD, const R* D
         launch_tiled<R>(1, P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(xi))),
                         cview(level_view(g, const_cast<R*>(b))), cview(level_view(g, const_cast<R*>(invD))),
                         cview(level_view(g, const_cast<R*>(D))), level_view(g, xo), omega, st);
+    else if (const MGLevel* sl = sizeof(R) == 4 ? op->split_for(reinterpret_cast<const float*>(C)) : nullptr)
+        launch_jacobi_split(P, sl->split, cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(C)))),
+                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(invD)))),
+                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(D)))),
+                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(xi)))),
+                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(b)))),
+                            level_view(g, reinterpret_cast<float*>(xo)), (float)omega, st,
+                            op->grains_for<float>(reinterpret_cast<const float*>(C)), sl->ngrains, op->dflag + 2);
     else
         launch_jacobi<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(invD))),
                          cview(level_view(g, const_cast<R*>(D))), cview(level_view(g, const_cast<R*>(xi))),
@@ -807,6 +866,7 @@ void solve_ml(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs
         throw;
     }
     cleanup();
+    check_tma_flag(op);
     int fails = 0;
     AE_CHECK(cudaMemcpyAsync(&fails, op->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     AE_CHECK(cudaStreamSynchronize(st));
@@ -907,14 +967,27 @@ int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) 
         op->st = op->own_st;
         if (const char* e = std::getenv("AE_TILED32")) op->tiled32 = std::atoi(e) != 0;
         if (const char* e = std::getenv("AE_TILED64")) op->tiled64 = std::atoi(e) != 0;
+        if (const char* e = std::getenv("AE_SPLIT")) op->split32 = std::atoi(e) != 0;
         tiled_init<float>();
         tiled_init<double>();
         AE_CHECK(cudaMallocHost(&op->hnorm, 8 * sizeof(unsigned long long)));
         op->dnorm = op->alloc<unsigned long long>(8);
         op->dflag = op->alloc<int>(4);
+        AE_CHECK(cudaMemsetAsync(op->dflag, 0, 4 * sizeof(int), op->st));
+        // row pitch: a multiple of 4 nodes on every level but AMR level 0's coarsest, whose
+        // bottom solve works on its dense layout (AE_PAD=0: dense everywhere)
+        bool pad = true;
+        if (const char* e = std::getenv("AE_PAD")) pad = std::atoi(e) != 0;
+        for (size_t a = 0; a < op->amr.size(); ++a)
+            for (size_t m = 0; m < op->amr[a].mg.size(); ++m) {
+                Geo& g = op->amr[a].mg[m].g;
+                const int nx = g.vhi[0] - g.vlo[0] + 1 + 2 * g.ng;
+                const bool bottom = a == 0 && m + 1 == op->amr[a].mg.size();
+                g.px = (pad && !bottom && nx >= 16) ? (nx + 3) / 4 * 4 : 0;
+            }
         for (auto& A : op->amr) {
             for (auto& L : A.mg) {
-                L.nn = box_npts(geo_store(L.g));
+                L.nn = geo_nn(L.g);
                 L.C = op->alloc<double>(op->ncoef * L.nn);
                 L.D = op->alloc<double>(3 * L.nn);
                 L.invD = op->alloc<double>(3 * L.nn);
@@ -1245,6 +1318,7 @@ int ae_fsmooth(ae_op* op, int amrlev, int mglev, const ae_fab* x, const ae_fab* 
                 std::swap(a, t);
             }
             launch_copy<R, R>(need, 3, fab_view<R>(*x), cview(level_view(L.g, a)), op->st);
+            check_tma_flag(op);
         };
         if (!x->is_float) {
             run(0.0);
@@ -1547,6 +1621,7 @@ int ae_profile_kernel(ae_op* op, int which, int amrlev, int mglev, int precision
         AE_CHECK(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        check_tma_flag(op);
         *avg_ms = (double)ms / reps;
     });
 }

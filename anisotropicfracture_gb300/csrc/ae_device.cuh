@@ -32,6 +32,8 @@ struct Geo {
     int dlo[3], dhi[3];  // nodal problem domain (inclusive)
     int vlo[3], vhi[3];  // nodal valid box
     int ng;              // ghost layers stored: storage box = grow(valid, ng)
+    int px = 0;          // row pitch of the level's internal arrays in nodes (0: the storage box's
+                         // x-extent); padded to a multiple of 4 so rows start on 16-byte boundaries
     double dx[3];
 };
 

@@ -172,17 +172,12 @@ __global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_residual(
 }
 
 // ------------------------------------------------------------------ damped Jacobi sweep
-// src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in.
+// src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in: one node (i, j, k).
 template <int M, class R, bool GR, bool SAME>
-__global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_jacobi(OpParams P, SCoef<R> K, Reg reg,
-                                                                               View<const R> C, Grains<R> G,
-                                                                               View<const R> invD, View<const R> D,
-                                                                               View<const R> xi, View<const R> b,
-                                                                               View<R> xo, R omega) {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= reg.n) return;
-    int i, j, k;
-    reg_ijk(reg, t, i, j, k);
+__device__ __forceinline__ void jacobi_node(const OpParams& P, const SCoef<R>& K, const View<const R>& C,
+                                            const Grains<R>& G, const View<const R>& invD, const View<const R>& D,
+                                            const View<const R>& xi, const View<const R>& b, const View<R>& xo,
+                                            R omega, int i, int j, int k) {
     const Geo& g = P.g;
     // SAME: every view has the layout of xi (checked by the launcher)
     const long long ox = xi.at(i, j, k), oo = SAME ? ox : xo.at(i, j, k);
@@ -217,6 +212,19 @@ __global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_jacobi(Op
             xo.p[oo + n * osc] = xv + omega * (b.p[ob + n * bsc] - v[n]) * invD.p[od + n * isc];
         }
     }
+}
+
+template <int M, class R, bool GR, bool SAME>
+__global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_jacobi(OpParams P, SCoef<R> K, Reg reg,
+                                                                               View<const R> C, Grains<R> G,
+                                                                               View<const R> invD, View<const R> D,
+                                                                               View<const R> xi, View<const R> b,
+                                                                               View<R> xo, R omega) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    jacobi_node<M, R, GR, SAME>(P, K, C, G, invD, D, xi, b, xo, omega, i, j, k);
 }
 
 // ------------------------------------------------------------------ z-marching tiled stencil sweeps

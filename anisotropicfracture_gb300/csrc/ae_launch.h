@@ -75,10 +75,17 @@ View<T> level_view(const Geo& g, T* p) {
     View<T> v;
     v.p = p;
     for (int d = 0; d < 3; ++d) v.lo[d] = s.lo[d];
-    v.sy = s.hi[0] - s.lo[0] + 1;
+    v.sy = g.px > 0 ? g.px : s.hi[0] - s.lo[0] + 1;
     v.sz = v.sy * (s.hi[1] - s.lo[1] + 1);
     v.sc = v.sz * (s.hi[2] - s.lo[2] + 1);
     return v;
+}
+// elements per component of a level's internal arrays (padding included)
+inline long long geo_nn(const Geo& g) {
+    const Box3 s = geo_store(g);
+    if (box_empty(s)) return 0;
+    const long long nx = g.px > 0 ? g.px : s.hi[0] - s.lo[0] + 1;
+    return nx * (s.hi[1] - s.lo[1] + 1) * (s.hi[2] - s.lo[2] + 1);
 }
 template <class T>
 View<const T> cview(const View<T>& v) {

@@ -1,0 +1,471 @@
+// Split FP32 sweeps on Voronoi (grain-map) levels.
+//
+// On a grain-map level the per-node sweep spends most of its issue slots on work that few nodes
+// need -- the domain-boundary classification, six neighbour grain ids, the grad C branch that
+// only the nodes whose stencil straddles a grain boundary take -- and waits on scattered loads.
+// A sweep there is split by node:
+//
+//   k_jacobi_tile  every node of the interior box I (not on the domain boundary, inside
+//                  grow(valid, 1)).  A block owns a 32 x 8 column of (i, j) and marches in k.
+//                  Per plane one elected thread loads, with TMA (cp.async.bulk.tensor) onto an
+//                  mbarrier, the x halo tile (three components), b, 1/D and the grain id/mask
+//                  tile of the next plane, so every read of the stencil and the update is a
+//                  shared-memory load at a fixed offset.  The grain table sits in shared memory.
+//                  The grad C term is computed only where the node's mask says a direction's two
+//                  neighbours lie in different grains.
+//   k_jacobi_list  every node of the sweep region outside I (domain-boundary rows, the ghost
+//                  ring, nodes outside the domain), through the per-node code (jacobi_node).
+//
+// Every node is computed by the per-node sweep's own arithmetic: where a direction's neighbours
+// share a grain the grad C column is exactly zero, and the interior and grad C expressions are
+// written operation for operation as apply_node_grains writes them, so the split sweep equals the
+// one-pass sweep bit for bit.  The list and the id/mask array are built once per level
+// (k_split_mark), when the FP32 copies are made.  TMA needs 16-byte aligned rows: the level
+// arrays' row pitch is a multiple of 4 nodes (Geo::px).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+#include <type_traits>
+
+#include "ae_kernels.cuh"
+#include "ae_split.h"
+
+namespace ae {
+
+namespace {
+
+constexpr int STX = 32, STY = 8, SNT = STX * STY;
+constexpr int SBW = 40;                    // box width: 32 nodes + halo + alignment shift, 160 B
+constexpr int SXR = STY + 2;               // x tile rows (one-node halo in j)
+constexpr int SXP = SBW * SXR;             // floats per x component plane tile
+constexpr int SXS = 3 * SXP + 16;          // floats per x ring slot (a multiple of 128 bytes)
+constexpr int SVP = SBW * STY;             // floats per b / 1/D component tile (no halo)
+constexpr int SVS = 3 * SVP;               // floats per b / 1/D ring slot
+constexpr int SXRING = 4, SVRING = 2;      // x planes k-1, k, k+1 + the one in flight; b, 1/D, ids
+constexpr unsigned kXBytes = 3 * SXP * 4, kVBytes = SVS * 4, kGBytes = SVP * 4;
+constexpr int kWaitLimit = 1 << 20;        // try_wait polls before a wait is declared failed
+#ifndef AE_SPLIT_MIN_BLOCKS
+#define AE_SPLIT_MIN_BLOCKS 4
+#endif
+
+// shared memory of the tiled kernel, in floats: x ring, b ring, 1/D ring, id ring (every TMA
+// destination on a 128-byte boundary), two mbarriers, the grain table
+constexpr int kOffB = SXRING * SXS;
+constexpr int kOffD = kOffB + SVRING * SVS;
+constexpr int kOffG = kOffD + SVRING * SVS;
+constexpr int kOffBar = kOffG + SVRING * SVP;
+constexpr int kOffT = kOffBar + 4;
+static_assert((SXS * 4) % 128 == 0 && (SVS * 4) % 128 == 0 && (SVP * 4) % 128 == 0, "TMA slot alignment");
+static_assert((kOffB * 4) % 128 == 0 && (kOffD * 4) % 128 == 0 && (kOffG * 4) % 128 == 0, "TMA ring alignment");
+constexpr int kTabSmemMax = 24 * 1024;  // bytes of grain table kept in shared memory
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for a phase of the barrier: false when it did not complete within kWaitLimit polls
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// 4-D tiled TMA load (x, y, z, component) into shared memory, completing on an mbarrier
+__device__ __forceinline__ void tma_load4(unsigned dst, const CUtensorMap* map, int x, int y, int z, int c,
+                                          unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(c), "r"(bar)
+        : "memory");
+}
+
+// packed node of a list: offsets from the storage box's low corner, 21 bits each
+__device__ __forceinline__ unsigned long long pack_node(int di, int dj, int dk) {
+    return (unsigned long long)di | ((unsigned long long)dj << 21) | ((unsigned long long)dk << 42);
+}
+__device__ __forceinline__ void unpack_node(unsigned long long c, const int lo[3], int& i, int& j, int& k) {
+    i = lo[0] + (int)(c & 0x1fffffull);
+    j = lo[1] + (int)((c >> 21) & 0x1fffffull);
+    k = lo[2] + (int)((c >> 42) & 0x1fffffull);
+}
+
+// Mark the nodes of the storage box outside the interior box I, which the list kernel computes,
+// and compact them (FILL = false: count only; order within a block follows the node order).
+// With FILL, also write gidm = gid | mask << 16 for every stored node, mask bit d set (nodes of I
+// only) when the two neighbours in direction d lie in different grains: a non-zero grad C column.
+template <bool FILL>
+__global__ void __launch_bounds__(kBlock) k_split_mark(Reg reg, Box3 I, View<const unsigned short> gid,
+                                                       unsigned* gidm, unsigned long long* list,
+                                                       unsigned long long* count) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool f = false;
+    unsigned long long code = 0;
+    if (t < reg.n) {
+        int i, j, k;
+        reg_ijk(reg, t, i, j, k);
+        const long long o = gid.at(i, j, k);
+        if (!in_box(I.lo, I.hi, i, j, k)) {
+            f = true;
+            if (FILL) gidm[o] = gid.p[o];
+        } else if (FILL) {
+            const long long off[3] = {1, gid.sy, gid.sz};
+            unsigned mask = 0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) mask |= (gid.p[o + off[d]] != gid.p[o - off[d]]) ? (1u << d) : 0u;
+            gidm[o] = (unsigned)gid.p[o] | (mask << 16);
+        }
+        code = pack_node(i - reg.lo[0], j - reg.lo[1], k - reg.lo[2]);
+    }
+    __shared__ unsigned wcnt[kBlock / 32];
+    __shared__ unsigned long long base;
+    const unsigned ball = __ballot_sync(0xffffffffu, f);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) wcnt[w] = __popc(ball);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int q = 0; q < kBlock / 32; ++q) {
+            const unsigned c = wcnt[q];
+            wcnt[q] = tot;
+            tot += c;
+        }
+        base = tot ? atomicAdd(count, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    if (FILL && f) list[base + wcnt[w] + __popc(ball & ((1u << lane) - 1u))] = code;
+}
+
+// Tile geometry shared by the host and the kernel: tensor coordinates are offsets from the
+// storage box's low corner; the boxes of a tile start at column xa (a multiple of 4, as TMA
+// requires), and node i of the tile sits at column sh + 1 + (i - i0).
+struct TileGeo {
+    Box3 I;        // interior box (absolute node indices)
+    int slo[3];    // storage box low corner
+    int tiles_x;   // tiles per row of I
+    int kz;        // planes per block
+    int sh;        // column shift of the tile's first halo column inside the box
+};
+
+// Damped-Jacobi sweep on the interior box I of a grain-map level (FP32): x_out = x + w (b - A x)/D
+// with A the interior row of Elastic<T>::Fapply.  gidm: grain id (low 16 bits) and the
+// directions with a non-zero grad C column (bits 16-18).  TABS: grain table in shared memory
+// (tab_n floats) or read through L1.  err: set when a TMA load did not complete.
+template <int M, bool TABS>
+__global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
+    k_jacobi_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
+                  const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_g, SCoef<float> K,
+                  TileGeo T, int uniform, long long sy, long long sz, long long sc,
+                  const unsigned* __restrict__ gidm_g, const float* __restrict__ tab, int tab_n, float* __restrict__ xo,
+                  float omega, int* err) {
+    constexpr int NC = NCoef<M>::value;
+    extern __shared__ __align__(128) float smem[];
+    const unsigned* gring = reinterpret_cast<const unsigned*>(smem + kOffG);
+    const float* tb = tab;
+    if (TABS) {
+        float* ts = smem + kOffT;
+        for (int q = threadIdx.x; q < tab_n; q += SNT) ts[q] = __ldg(tab + q);
+        tb = ts;
+    }
+    const int tx = threadIdx.x % STX, ty = threadIdx.x / STX;
+    const int i0 = T.I.lo[0] + (int)(blockIdx.x % T.tiles_x) * STX, j0 = T.I.lo[1] + (int)(blockIdx.x / T.tiles_x) * STY;
+    const int k0 = T.I.lo[2] + (int)blockIdx.y * T.kz;
+    const int k1 = min(k0 + T.kz - 1, T.I.hi[2]);
+    const int i = i0 + tx, j = j0 + ty;
+    const bool act = i <= T.I.hi[0] && j <= T.I.hi[1];
+    // tensor coordinates of the boxes
+    const int xa = i0 - 1 - T.slo[0] - T.sh;
+    const int yx = j0 - 1 - T.slo[1], yv = j0 - T.slo[1];
+    const unsigned sb = smem_u32(smem);
+    const unsigned bar0 = sb + 4u * kOffBar;
+    const bool leader = threadIdx.x == 0;
+    if (leader) {
+        mbar_init(bar0, 1);
+        mbar_init(bar0 + 8, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto load_x = [&](int k, unsigned bar) {
+        tma_load4(sb + 4u * (unsigned)((k & 3) * SXS), &tm_x, xa, yx, k - T.slo[2], 0, bar);
+    };
+    auto load_v = [&](int k, unsigned bar) {
+        const unsigned s = (unsigned)(k & 1);
+        tma_load4(sb + 4u * (kOffB + s * SVS), &tm_b, xa, yv, k - T.slo[2], 0, bar);
+        tma_load4(sb + 4u * (kOffD + s * SVS), &tm_d, xa, yv, k - T.slo[2], 0, bar);
+        tma_load4(sb + 4u * (kOffG + s * SVP), &tm_g, xa, yv, k - T.slo[2], 0, bar);
+    };
+    // stage 0: planes k0-1, k0, k0+1 of x and the b, 1/D, id tiles of plane k0
+    if (leader) {
+        mbar_expect_tx(bar0, 3 * kXBytes + 2 * kVBytes + kGBytes);
+        load_x(k0 - 1, bar0);
+        load_x(k0, bar0);
+        load_x(k0 + 1, bar0);
+        load_v(k0, bar0);
+    }
+    const int col = T.sh + 1 + tx;
+    const int cx = (ty + 1) * SBW + col;  // this node inside an x component tile
+    const int cv = ty * SBW + col;        // ... inside a b / 1/D / id component tile
+    long long o = (long long)(i - T.slo[0]) + (long long)(j - T.slo[1]) * sy + (long long)(k0 - T.slo[2]) * sz;
+    bool failed = false;
+    int last = 0;  // last stage issued
+    for (int k = k0; k <= k1; ++k, o += sz) {
+        const int s = k - k0;
+        // stage s + 1: plane k + 2 of x and the tiles of plane k + 1; their ring slots were last
+        // read in iteration k - 1, which the barrier at its end closed
+        if (k + 1 <= k1) {
+            last = s + 1;
+            if (leader) {
+                const unsigned bn = bar0 + 8u * (unsigned)((s + 1) & 1);
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                mbar_expect_tx(bn, kXBytes + 2 * kVBytes + kGBytes);
+                load_x(k + 2, bn);
+                load_v(k + 1, bn);
+            }
+        }
+        const bool ok = mbar_wait(bar0 + 8u * (unsigned)(s & 1), (unsigned)((s >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        if (act) {
+            const float* pm = smem + ((k - 1) & 3) * SXS + cx;
+            const float* pc = smem + (k & 3) * SXS + cx;
+            const float* pp = smem + ((k + 1) & 3) * SXS + cx;
+            const unsigned vs = (unsigned)(k & 1);
+            const unsigned gw = gring[vs * SVP + cv];
+            float bb[3][3][3], xv[3];
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                const float* um = pm + p * SXP;
+                const float* uc = pc + p * SXP;
+                const float* up = pp + p * SXP;
+                const float c0 = uc[0];
+                xv[p] = c0;
+                const float xm = uc[-1], xp = uc[1], ym = uc[-SBW], yp = uc[SBW], zm = um[0], zp = up[0];
+                bb[p][0][0] = (xp - 2.0f * c0 + xm) * K.i2[0];
+                bb[p][1][1] = (yp - 2.0f * c0 + ym) * K.i2[1];
+                bb[p][2][2] = (zp - 2.0f * c0 + zm) * K.i2[2];
+                bb[p][0][1] = (uc[1 + SBW] + uc[-1 - SBW] - uc[1 - SBW] - uc[-1 + SBW]) * K.m01;
+                bb[p][0][2] = (up[1] + um[-1] - um[1] - up[-1]) * K.m02;
+                bb[p][1][2] = (up[SBW] + um[-SBW] - um[SBW] - up[-SBW]) * K.m12;
+                bb[p][1][0] = bb[p][0][1];
+                bb[p][2][0] = bb[p][0][2];
+                bb[p][2][1] = bb[p][1][2];
+            }
+            float f[3];
+            {
+                float a[NC];
+                const float* a0 = tb + (int)(gw & 0xffffu) * NC;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) a[q] = a0[q];
+                div_of<M, float>(a, bb, f);
+            }
+            const unsigned mask = gw >> 16;
+            if (!uniform && mask) {
+                float gu[3][3];
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {
+                    const float* um = pm + p * SXP;
+                    const float* uc = pc + p * SXP;
+                    const float* up = pp + p * SXP;
+                    gu[p][0] = (uc[1] - uc[-1]) * K.h[0];
+                    gu[p][1] = (uc[SBW] - uc[-SBW]) * K.h[1];
+                    gu[p][2] = (up[0] - um[0]) * K.h[2];
+                }
+                // neighbour ids: x from the tile, y from the tile inside it, the rest from global
+                const unsigned* gv = gring + vs * SVP + cv;
+                const int gid_n[3][2] = {
+                    {(int)(gv[1] & 0xffffu), (int)(gv[-1] & 0xffffu)},
+                    {(int)((ty + 1 < STY ? gv[SBW] : __ldg(gidm_g + o + sy)) & 0xffffu),
+                     (int)((ty > 0 ? gv[-SBW] : __ldg(gidm_g + o - sy)) & 0xffffu)},
+                    {(int)(__ldg(gidm_g + o + sz) & 0xffffu), (int)(__ldg(gidm_g + o - sz) & 0xffffu)}};
+                float colv[3][3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (mask & (1u << d)) {
+                        const float* cp = tb + gid_n[d][0] * NC;
+                        const float* cm = tb + gid_n[d][1] * NC;
+                        gradC_col_f<M, float>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
+                    } else {
+                        colv[d][0] = colv[d][1] = colv[d][2] = 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 3; ++r) f[r] += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
+            }
+            const float* bv = smem + kOffB + vs * SVS + cv;
+            const float* dv = smem + kOffD + vs * SVS + cv;
+#pragma unroll
+            for (int n = 0; n < 3; ++n) xo[o + n * sc] = xv[n] + omega * (bv[n * SVP] - f[n]) * dv[n * SVP];
+        }
+        __syncthreads();
+    }
+    if (failed) {
+        if (leader) atomicExch(err, 1);
+        // loads still in flight may land: wait (bounded) for the stages issued before leaving
+        for (int s = max(last - 1, 0); s <= last; ++s) mbar_wait(bar0 + 8u * (unsigned)(s & 1), (unsigned)((s >> 1) & 1));
+    }
+}
+
+// 4 resident blocks (64 registers): at 48 the cubic variant spills
+template <int M, bool SAME>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_jacobi_list(OpParams P, SCoef<float> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
+                  View<const float> C, Grains<float> G, View<const float> invD, View<const float> D,
+                  View<const float> xi, View<const float> b, View<float> xo, float omega) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_node(list[t], S.lo, i, j, k);
+    jacobi_node<M, float, true, SAME>(P, K, C, G, invD, D, xi, b, xo, omega, i, j, k);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    if (!fn) throw std::runtime_error("cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+// Tensor map over a level array [comp][k][j][i] (storage box, row pitch px), boxes of
+// SBW x rows x 1 x ncomp elements of 4 bytes.
+CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUtensorMapDataType type) {
+    const Box3 s = geo_store(g);
+    const cuuint64_t nx = (cuuint64_t)(s.hi[0] - s.lo[0] + 1), ny = (cuuint64_t)(s.hi[1] - s.lo[1] + 1),
+                     nz = (cuuint64_t)(s.hi[2] - s.lo[2] + 1);
+    const cuuint64_t px = (cuuint64_t)g.px;
+    const cuuint64_t dims[4] = {nx, ny, nz, (cuuint64_t)ncomp};
+    const cuuint64_t strides[3] = {px * 4, px * ny * 4, px * ny * nz * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)SBW, (cuuint32_t)rows, 1, (cuuint32_t)ncomp};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUtensorMap m;
+    const CUresult r = encode_fn()(&m, type, 4, const_cast<void*>(base), dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return m;
+}
+
+size_t tile_smem(int tab_n, bool tabs) { return sizeof(float) * (size_t)(kOffT + (tabs ? tab_n : 0)); }
+
+template <int M, bool TABS>
+void tile_smem_attr(size_t bytes) {
+    static size_t set = 0;
+    if (bytes > set) {
+        AE_CUDA_CHECK(cudaFuncSetAttribute(k_jacobi_tile<M, TABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bytes));
+        set = bytes;
+    }
+}
+
+}  // namespace
+
+Box3 split_interior(const Geo& g) {
+    Box3 d = geo_domain(g);
+    for (int q = 0; q < 3; ++q) { d.lo[q] += 1; d.hi[q] -= 1; }
+    return box_isect(box_isect(box_grow(geo_valid(g), 1), d), box_grow(geo_store(g), -1));
+}
+
+bool split_supported(const Geo& g) {
+    if (g.px <= 0 || g.px % 4 != 0) return false;
+    const Box3 S = geo_store(g);
+    for (int q = 0; q < 3; ++q)
+        if (S.hi[q] - S.lo[q] >= (1 << 21)) return false;
+    return true;
+}
+
+long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& sl, cudaStream_t st,
+                      unsigned long long* scratch_count) {
+    if (!split_supported(g)) throw std::runtime_error("split sweep: level layout not supported");
+    const Box3 S = geo_store(g);
+    const Reg reg = make_reg(S);
+    const Box3 I = split_interior(g);
+    AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
+    k_split_mark<false><<<nblocks(reg.n), kBlock, 0, st>>>(reg, I, gid, nullptr, nullptr, scratch_count);
+    launched();
+    unsigned long long n = 0;
+    AE_CUDA_CHECK(cudaMemcpyAsync(&n, scratch_count, sizeof(n), cudaMemcpyDeviceToHost, st));
+    AE_CUDA_CHECK(cudaStreamSynchronize(st));
+    AE_CUDA_CHECK(cudaMalloc(&sl.gidm, sizeof(unsigned) * (size_t)geo_nn(g)));
+    AE_CUDA_CHECK(cudaMemsetAsync(sl.gidm, 0, sizeof(unsigned) * (size_t)geo_nn(g), st));
+    if (n > 0) AE_CUDA_CHECK(cudaMalloc(&sl.list, sizeof(unsigned long long) * n));
+    AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
+    k_split_mark<true><<<nblocks(reg.n), kBlock, 0, st>>>(reg, I, gid, sl.gidm, sl.list, scratch_count);
+    launched();
+    AE_CUDA_CHECK(cudaStreamSynchronize(st));
+    sl.n = (long long)n;
+    return sl.n;
+}
+
+void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
+                         View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
+                         cudaStream_t st, Grains<float> G, int ngrains, int* err) {
+    const SCoef<float> K = make_scoef<float>(P.g);
+    const Box3 S = geo_store(P.g);
+    const Box3 I = split_interior(P.g);
+    const bool same = same_layout(xi, C) && same_layout(xi, invD) && same_layout(xi, D) && same_layout(xi, b) &&
+                      same_layout(xi, xo);
+    if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
+    dispatch_model<float>(P.model, [&](auto m) {
+        constexpr int Mv = decltype(m)::value;
+        if (!box_empty(I)) {
+            TileGeo T;
+            T.I = I;
+            for (int q = 0; q < 3; ++q) T.slo[q] = S.lo[q];
+            const int nx = I.hi[0] - I.lo[0] + 1, ny = I.hi[1] - I.lo[1] + 1, nz = I.hi[2] - I.lo[2] + 1;
+            T.tiles_x = (nx + STX - 1) / STX;
+            const int tiles_y = (ny + STY - 1) / STY;
+            T.kz = sl.kz > 0 ? sl.kz : 16;
+            // every tile starts 32 nodes after the previous one, so one shift serves all of them
+            T.sh = (I.lo[0] - 1 - S.lo[0]) & 3;
+            const CUtensorMap tx = level_tmap(xi.p, P.g, 3, SXR, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+            const CUtensorMap tb = level_tmap(b.p, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+            const CUtensorMap td = level_tmap(invD.p, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+            const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32);
+            const dim3 grid((unsigned)(T.tiles_x * tiles_y), (unsigned)((nz + T.kz - 1) / T.kz));
+            const int tab_n = ngrains * NCoef<Mv>::value;
+            const bool tabs = tab_n * (int)sizeof(float) <= kTabSmemMax;
+            const size_t smem = tile_smem(tab_n, tabs);
+            if (tabs) {
+                tile_smem_attr<Mv, true>(smem);
+                k_jacobi_tile<Mv, true><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, xi.sy, xi.sz, xi.sc,
+                                                                  sl.gidm, G.tab, tab_n, xo.p, omega, err);
+            } else {
+                tile_smem_attr<Mv, false>(smem);
+                k_jacobi_tile<Mv, false><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, xi.sy, xi.sz,
+                                                                   xi.sc, sl.gidm, G.tab, tab_n, xo.p, omega, err);
+            }
+            launched();
+        }
+        if (sl.n > 0) {
+            k_jacobi_list<Mv, true><<<(unsigned)((sl.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+                P, K, sl.list, sl.n, S, C, G, invD, D, xi, b, xo, omega);
+            launched();
+        }
+    });
+}
+
+}  // namespace ae

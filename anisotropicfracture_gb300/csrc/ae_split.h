@@ -1,0 +1,36 @@
+// Split FP32 sweeps on Voronoi (grain-map) levels: a tiled kernel over the interior box plus
+// the per-node code over a list of the nodes that need it (see ae_split.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ae_launch.h"
+
+namespace ae {
+
+struct SplitList {
+    unsigned long long* list = nullptr;  // nodes outside the interior box: packed offsets from the
+                                         // storage box's low corner
+    long long n = 0;
+    unsigned* gidm = nullptr;            // per stored node: grain id | grad C directions << 16
+    int kz = 0;                          // planes per block of the tiled kernel (0: default 16)
+};
+// grain ids the split sweep can carry next to its 3-bit direction mask
+constexpr int kSplitMaxGrains = 1 << 16;
+
+// Interior box of the tiled kernel: grow(valid, 1) without the domain's boundary nodes, with a
+// one-node halo inside the storage box.
+Box3 split_interior(const Geo& g);
+// whether a level's layout allows the split sweep (row pitch a multiple of 4 nodes)
+bool split_supported(const Geo& g);
+// Build the node list and the id/mask array of a grain-map level (gid laid out like the level's
+// storage, at most kSplitMaxGrains grains); allocates sl.list and sl.gidm with cudaMalloc and
+// returns the list's length.  scratch_count: one device counter.  Synchronises the stream.
+long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& sl, cudaStream_t st,
+                      unsigned long long* scratch_count);
+// One damped-Jacobi sweep (FP32) of a grain-map level: the tiled interior kernel, then the list.
+// *err is set (device) when a TMA load of the tiled kernel did not complete.
+void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
+                         View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
+                         cudaStream_t st, Grains<float> G, int ngrains, int* err);
+
+}  // namespace ae

@@ -1,0 +1,136 @@
+"""The split FP32 sweep on grain-map levels (ae_split.cu: a TMA-staged tiled kernel over the
+interior box plus the per-node code over the boundary shell) against the one-pass per-node sweep
+(AE_SPLIT=0, read when an operator is created).  Every node is computed with the per-node sweep's
+own arithmetic, so the results must be equal bit for bit (tolerance 0): FP32 Fsmooth on a single
+level of odd size (partial tiles, anisotropic spacing) and on refined patches with ghost layers
+(inside the domain, and touching its low faces), m_uniform on and off, random BC tables, and
+whole mixed-precision solves.  Also: the padded row pitch of the level arrays (AE_PAD=0: dense)
+changes no result."""
+import os
+
+import numpy as np
+import pytest
+
+from anisotropicfracture_gb300 import microstructure, models
+from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
+from helpers import bc_random, polycrystal_amr
+from oracle import pyoracle as po
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _descs(Ls):
+    return [level_desc(tuple(L.dom_hi[d] for d in range(3)), lo=tuple(L.lo), hi=tuple(L.hi), dx=tuple(L.dx))
+            for L in Ls]
+
+
+def _lo(L):
+    return tuple(L.lo[d] - L.ng for d in range(3))
+
+
+def _grains(Ls, ngr=12, seed=9):
+    seeds = microstructure.voronoi_seeds(ngr, seed)
+    tab = models.cubic(1.68, 1.21, 0.75, models.random_rotations(ngr, np.random.default_rng(seed + 1)))
+    gids = []
+    for L in Ls:
+        lo = [L.lo[d] - L.ng for d in range(3)]
+        hi = [L.hi[d] + L.ng for d in range(3)]
+        g = microstructure.voronoi_grain_ids(lo, hi, tuple(L.dx), seeds).astype(np.int32)
+        gids.append(np.ascontiguousarray(g[None]))
+    return gids, tab
+
+
+def _op(split, Ls, bc, gids, tab, uniform, pad=True):
+    os.environ["AE_SPLIT"] = "1" if split else "0"
+    os.environ["AE_PAD"] = "1" if pad else "0"
+    try:
+        op = Elastic(_descs(Ls), models.MAJORMINOR)
+    finally:
+        os.environ.pop("AE_SPLIT", None)
+        os.environ.pop("AE_PAD", None)
+    for l, L in enumerate(Ls):
+        op.SetModelGrains(l, Field(gids[l], _lo(L)), tab)
+    op.SetBC(bc)
+    op.SetUniform(uniform)
+    op.prepareForSolve()
+    return op
+
+
+def _fsmooth(op, a, L, x, b, sweeps):
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    bd = torch.from_numpy(b.astype(np.float32)).cuda()
+    op.Fsmooth(a, 0, Field(xd, _lo(L)), Field(bd, _lo(L)), sweeps, 2.0 / 3.0)
+    torch.cuda.synchronize()
+    return xd.cpu().numpy()
+
+
+@pytest.mark.parametrize("uniform", [False, True])
+def test_split_sweep_equals_per_node_single_level(uniform):
+    Ls = [po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))]
+    gids, tab = _grains(Ls)
+    rng = np.random.default_rng(1)
+    bc = bc_random(rng)
+    x = rng.standard_normal((3,) + Ls[0].shape)
+    b = rng.standard_normal((3,) + Ls[0].shape)
+    ref = _fsmooth(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3)
+    got = _fsmooth(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3)
+    assert np.array_equal(got, ref), int((got != ref).sum())
+
+
+@pytest.mark.parametrize("where", ["inside", "low_corner"])
+def test_split_sweep_equals_per_node_on_a_refined_patch(where):
+    if where == "inside":
+        Ls, _, bc, _ = polycrystal_amr(24, 2)
+    else:  # a patch whose ghost layers reach past the domain's low faces
+        Ls = [po.level(24), po.level(48, lo=(0, 0, 0), hi=(24, 24, 24), ng=2)]
+        bc = bc_random(np.random.default_rng(4))
+    gids, tab = _grains(Ls)
+    rng = np.random.default_rng(2)
+    for a, L in enumerate(Ls):
+        x = rng.standard_normal((3,) + L.shape)
+        b = rng.standard_normal((3,) + L.shape)
+        ref = _fsmooth(_op(False, Ls, bc, gids, tab, False, pad=False), a, L, x, b, 2)
+        got = _fsmooth(_op(True, Ls, bc, gids, tab, False), a, L, x, b, 2)
+        assert np.array_equal(got, ref), (a, int((got != ref).sum()))
+
+
+@pytest.mark.parametrize("nlev", [1, 2])
+def test_split_sweep_mixed_solve_equals_per_node(nlev):
+    Ls, Cs, bc, bs = polycrystal_amr(24, nlev)
+    gids, tab = _grains(Ls)
+    out = []
+    for split, pad in ((False, False), (True, True)):
+        op = _op(split, Ls, bc, gids, tab, False, pad)
+        s = Linear(op)
+        s.setMaxFmgIter(0)
+        s.setBottomSolver("cg")
+        s.setPreSmooth(1)
+        s.setPostSmooth(1)
+        s.setPrecision("mixed")
+        s.opts.inner_cycles = 4
+        xs = [np.zeros_like(b) for b in bs]
+        s.solve([Field(x, _lo(L)) for x, L in zip(xs, Ls)], [Field(b, _lo(L)) for b, L in zip(bs, Ls)], 1e-8, 0.0)
+        assert s.stats.converged
+        out.append((s.stats.iters, xs))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+
+
+def test_padded_pitch_changes_no_fp64_result():
+    """The FP64 solve on the padded layout equals the dense layout bit for bit."""
+    Ls, Cs, bc, bs = polycrystal_amr(24, 2)
+    gids, tab = _grains(Ls)
+    sols = []
+    for pad in (False, True):
+        op = _op(False, Ls, bc, gids, tab, False, pad)
+        s = Linear(op)
+        s.setMaxFmgIter(0)
+        s.setPrecision("fp64")
+        xs = [np.zeros_like(b) for b in bs]
+        s.solve([Field(x, _lo(L)) for x, L in zip(xs, Ls)], [Field(b, _lo(L)) for b, L in zip(bs, Ls)], 1e-8, 0.0)
+        sols.append((s.stats.iters, xs))
+    assert sols[0][0] == sols[1][0]
+    for a, b in zip(sols[0][1], sols[1][1]):
+        assert np.array_equal(a, b)
