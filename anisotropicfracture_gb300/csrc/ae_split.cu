@@ -56,7 +56,9 @@ constexpr int kOffB = SXRING * SXS;
 constexpr int kOffD = kOffB + SVRING * SVS;
 constexpr int kOffG = kOffD + SVRING * SVS;
 constexpr int kOffBar = kOffG + SVRING * SVP;
-constexpr int kOffT = kOffBar + 4;
+// queue of the plane's nodes with a non-zero grad C column: count, thread index, main-term f
+constexpr int kOffQ = kOffBar + 4;
+constexpr int kOffT = kOffQ + 4 + SNT + 3 * SNT;
 static_assert((SXS * 4) % 128 == 0 && (SVS * 4) % 128 == 0 && (SVP * 4) % 128 == 0, "TMA slot alignment");
 static_assert((kOffB * 4) % 128 == 0 && (kOffD * 4) % 128 == 0 && (kOffG * 4) % 128 == 0, "TMA ring alignment");
 constexpr int kTabSmemMax = 24 * 1024;  // bytes of grain table kept in shared memory
@@ -175,6 +177,9 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     constexpr int NC = NCoef<M>::value;
     extern __shared__ __align__(128) float smem[];
     const unsigned* gring = reinterpret_cast<const unsigned*>(smem + kOffG);
+    int* qn = reinterpret_cast<int*>(smem + kOffQ);
+    int* qtid = qn + 4;
+    float* qf = smem + kOffQ + 4 + SNT;
     const float* tb = tab;
     if (TABS) {
         float* ts = smem + kOffT;
@@ -194,6 +199,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     const unsigned bar0 = sb + 4u * kOffBar;
     const bool leader = threadIdx.x == 0;
     if (leader) {
+        *qn = 0;
         mbar_init(bar0, 1);
         mbar_init(bar0 + 8, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -241,13 +247,17 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             failed = true;
             break;
         }
+        const unsigned vs = (unsigned)(k & 1);
+        const float* pm = smem + ((k - 1) & 3) * SXS + cx;
+        const float* pc = smem + (k & 3) * SXS + cx;
+        const float* pp = smem + ((k + 1) & 3) * SXS + cx;
+        const float* bv = smem + kOffB + vs * SVS + cv;
+        const float* dv = smem + kOffD + vs * SVS + cv;
+        bool queued = false;
+        float f[3], xv[3];
         if (act) {
-            const float* pm = smem + ((k - 1) & 3) * SXS + cx;
-            const float* pc = smem + (k & 3) * SXS + cx;
-            const float* pp = smem + ((k + 1) & 3) * SXS + cx;
-            const unsigned vs = (unsigned)(k & 1);
             const unsigned gw = gring[vs * SVP + cv];
-            float bb[3][3][3], xv[3];
+            float bb[3][3][3];
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 const float* um = pm + p * SXP;
@@ -266,7 +276,6 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                 bb[p][2][0] = bb[p][0][2];
                 bb[p][2][1] = bb[p][1][2];
             }
-            float f[3];
             {
                 float a[NC];
                 const float* a0 = tb + (int)(gw & 0xffffu) * NC;
@@ -274,45 +283,78 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                 for (int q = 0; q < NC; ++q) a[q] = a0[q];
                 div_of<M, float>(a, bb, f);
             }
-            const unsigned mask = gw >> 16;
-            if (!uniform && mask) {
-                float gu[3][3];
-#pragma unroll
-                for (int p = 0; p < 3; ++p) {
-                    const float* um = pm + p * SXP;
-                    const float* uc = pc + p * SXP;
-                    const float* up = pp + p * SXP;
-                    gu[p][0] = (uc[1] - uc[-1]) * K.h[0];
-                    gu[p][1] = (uc[SBW] - uc[-SBW]) * K.h[1];
-                    gu[p][2] = (up[0] - um[0]) * K.h[2];
+            queued = !uniform && (gw >> 16) != 0;
+        }
+        // nodes with a grad C column go to the plane's queue (one shared-memory atomic per warp);
+        // the others are finished here
+        {
+            const unsigned ball = __ballot_sync(0xffffffffu, queued);
+            int base = 0;
+            if (ball) {
+                const int lane = threadIdx.x & 31;
+                if (lane == __ffs(ball) - 1) base = atomicAdd(qn, __popc(ball));
+                base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
+                if (queued) {
+                    const int e = base + __popc(ball & ((1u << lane) - 1u));
+                    qtid[e] = (int)threadIdx.x;
+                    qf[3 * e] = f[0];
+                    qf[3 * e + 1] = f[1];
+                    qf[3 * e + 2] = f[2];
                 }
-                // neighbour ids: x from the tile, y from the tile inside it, the rest from global
-                const unsigned* gv = gring + vs * SVP + cv;
-                const int gid_n[3][2] = {
-                    {(int)(gv[1] & 0xffffu), (int)(gv[-1] & 0xffffu)},
-                    {(int)((ty + 1 < STY ? gv[SBW] : __ldg(gidm_g + o + sy)) & 0xffffu),
-                     (int)((ty > 0 ? gv[-SBW] : __ldg(gidm_g + o - sy)) & 0xffffu)},
-                    {(int)(__ldg(gidm_g + o + sz) & 0xffffu), (int)(__ldg(gidm_g + o - sz) & 0xffffu)}};
-                float colv[3][3];
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    if (mask & (1u << d)) {
-                        const float* cp = tb + gid_n[d][0] * NC;
-                        const float* cm = tb + gid_n[d][1] * NC;
-                        gradC_col_f<M, float>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
-                    } else {
-                        colv[d][0] = colv[d][1] = colv[d][2] = 0.0f;
-                    }
-                }
-#pragma unroll
-                for (int r = 0; r < 3; ++r) f[r] += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
             }
-            const float* bv = smem + kOffB + vs * SVS + cv;
-            const float* dv = smem + kOffD + vs * SVS + cv;
+        }
+        if (act && !queued) {
 #pragma unroll
             for (int n = 0; n < 3; ++n) xo[o + n * sc] = xv[n] + omega * (bv[n * SVP] - f[n]) * dv[n * SVP];
         }
         __syncthreads();
+        // the queued nodes, one per thread: grad C columns of the directions whose neighbours lie in
+        // different grains, then the update
+        for (int e = threadIdx.x; e < *qn; e += SNT) {
+            const int t = qtid[e];
+            const int qx = t % STX, qy = t / STX;
+            const int qcx = (qy + 1) * SBW + T.sh + 1 + qx, qcv = qy * SBW + T.sh + 1 + qx;
+            const long long qo = o + (long long)(qx - tx) + (long long)(qy - ty) * sy;
+            const float* qm = smem + ((k - 1) & 3) * SXS + qcx;
+            const float* qc = smem + (k & 3) * SXS + qcx;
+            const float* qp = smem + ((k + 1) & 3) * SXS + qcx;
+            float gu[3][3];
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                gu[p][0] = (qc[p * SXP + 1] - qc[p * SXP - 1]) * K.h[0];
+                gu[p][1] = (qc[p * SXP + SBW] - qc[p * SXP - SBW]) * K.h[1];
+                gu[p][2] = (qp[p * SXP] - qm[p * SXP]) * K.h[2];
+            }
+            // neighbour ids: x from the tile, y from the tile inside it, the rest from global
+            const unsigned* gv = gring + vs * SVP + qcv;
+            const unsigned mask = gv[0] >> 16;
+            const int gid_n[3][2] = {
+                {(int)(gv[1] & 0xffffu), (int)(gv[-1] & 0xffffu)},
+                {(int)((qy + 1 < STY ? gv[SBW] : __ldg(gidm_g + qo + sy)) & 0xffffu),
+                 (int)((qy > 0 ? gv[-SBW] : __ldg(gidm_g + qo - sy)) & 0xffffu)},
+                {(int)(__ldg(gidm_g + qo + sz) & 0xffffu), (int)(__ldg(gidm_g + qo - sz) & 0xffffu)}};
+            float colv[3][3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (mask & (1u << d)) {
+                    const float* cp = tb + gid_n[d][0] * NC;
+                    const float* cm = tb + gid_n[d][1] * NC;
+                    gradC_col_f<M, float>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
+                } else {
+                    colv[d][0] = colv[d][1] = colv[d][2] = 0.0f;
+                }
+            }
+            const float* qb = smem + kOffB + vs * SVS + qcv;
+            const float* qd = smem + kOffD + vs * SVS + qcv;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                float fr = qf[3 * e + r];
+                fr += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
+                xo[qo + r * sc] = qc[r * SXP] + omega * (qb[r * SVP] - fr) * qd[r * SVP];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *qn = 0;
     }
     if (failed) {
         if (leader) atomicExch(err, 1);
