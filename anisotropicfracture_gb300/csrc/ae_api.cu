@@ -162,6 +162,7 @@ struct ae_op_s {
         for (auto& A : amr)
             for (auto& L : A.mg) {
                 if (L.split.list) cudaFree(L.split.list);
+                if (L.split.list_r) cudaFree(L.split.list_r);
                 if (L.split.gidm) cudaFree(L.split.gidm);
             }
         for (void* p : allocs) cudaFree(p);
@@ -455,6 +456,7 @@ void prepare(ae_op* op) {
     for (auto& A : op->amr)
         for (auto& L : A.mg) {
             if (L.split.list) AE_CHECK(cudaFree(L.split.list));
+            if (L.split.list_r) AE_CHECK(cudaFree(L.split.list_r));
             if (L.split.gidm) AE_CHECK(cudaFree(L.split.gidm));
             L.split = SplitList{};
             L.split_built = false;
@@ -507,6 +509,12 @@ void sweep_residual(ae_op* op, const Geo& g, const R* C, const R* x, const R* b,
         launch_tiled<R>(2, P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                         cview(level_view(g, const_cast<R*>(b))), cview(level_view(g, const_cast<R*>(b))),
                         cview(level_view(g, const_cast<R*>(b))), level_view(g, r), R(0), st);
+    else if (const MGLevel* sl = sizeof(R) == 4 ? op->split_for(reinterpret_cast<const float*>(C)) : nullptr)
+        launch_residual_split(P, sl->split, cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(C)))),
+                              cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(x)))),
+                              cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(b)))),
+                              level_view(g, reinterpret_cast<float*>(r)), st,
+                              op->grains_for<float>(reinterpret_cast<const float*>(C)), sl->ngrains, op->dflag + 2);
     else
         launch_residual<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                            cview(level_view(g, const_cast<R*>(b))), level_view(g, r), nullptr, nullptr, st,

@@ -5,7 +5,7 @@
 // only the nodes whose stencil straddles a grain boundary take -- and waits on scattered loads.
 // A sweep there is split by node:
 //
-//   k_jacobi_tile  every node of the interior box I (not on the domain boundary, inside
+//   k_sweep_tile   every node of the interior box I (not on the domain boundary, inside
 //                  grow(valid, 1)).  A block owns a 32 x 8 column of (i, j) and marches in k.
 //                  Per plane one elected thread loads, with TMA (cp.async.bulk.tensor) onto an
 //                  mbarrier, the x halo tile (three components), b, 1/D and the grain id/mask
@@ -13,8 +13,11 @@
 //                  shared-memory load at a fixed offset.  The grain table sits in shared memory.
 //                  The grad C term is computed only where the node's mask says a direction's two
 //                  neighbours lie in different grains.
-//   k_jacobi_list  every node of the sweep region outside I (domain-boundary rows, the ghost
-//                  ring, nodes outside the domain), through the per-node code (jacobi_node).
+//   k_*_list       every node of the sweep region outside I (domain-boundary rows, the ghost
+//                  ring, nodes outside the domain), through the per-node code.
+//
+// Two sweeps are split this way: the damped-Jacobi smoother and the correction residual
+// r = b - A x of the FP32 cycle.
 //
 // Every node is computed by the per-node sweep's own arithmetic: where a direction's neighbours
 // share a grain the grad C column is exactly zero, and the interior and grad C expressions are
@@ -106,12 +109,13 @@ __device__ __forceinline__ void unpack_node(unsigned long long c, const int lo[3
     k = lo[2] + (int)((c >> 42) & 0x1fffffull);
 }
 
-// Mark the nodes of the storage box outside the interior box I, which the list kernel computes,
-// and compact them (FILL = false: count only; order within a block follows the node order).
-// With FILL, also write gidm = gid | mask << 16 for every stored node, mask bit d set (nodes of I
-// only) when the two neighbours in direction d lie in different grains: a non-zero grad C column.
+// Mark the nodes of region R (inside the storage box) outside the interior box I, which a list
+// kernel computes, and compact them (FILL = false: count only; order within a block follows the
+// node order).  With FILL and gidm, also write gidm = gid | mask << 16 for every stored node, mask
+// bit d set (nodes of I only) when the two neighbours in direction d lie in different grains: a
+// non-zero grad C column.
 template <bool FILL>
-__global__ void __launch_bounds__(kBlock) k_split_mark(Reg reg, Box3 I, View<const unsigned short> gid,
+__global__ void __launch_bounds__(kBlock) k_split_mark(Reg reg, Box3 R, Box3 I, View<const unsigned short> gid,
                                                        unsigned* gidm, unsigned long long* list,
                                                        unsigned long long* count) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -122,9 +126,9 @@ __global__ void __launch_bounds__(kBlock) k_split_mark(Reg reg, Box3 I, View<con
         reg_ijk(reg, t, i, j, k);
         const long long o = gid.at(i, j, k);
         if (!in_box(I.lo, I.hi, i, j, k)) {
-            f = true;
-            if (FILL) gidm[o] = gid.p[o];
-        } else if (FILL) {
+            f = in_box(R.lo, R.hi, i, j, k);
+            if (FILL && gidm) gidm[o] = gid.p[o];
+        } else if (FILL && gidm) {
             const long long off[3] = {1, gid.sy, gid.sz};
             unsigned mask = 0;
 #pragma unroll
@@ -163,13 +167,16 @@ struct TileGeo {
     int sh;        // column shift of the tile's first halo column inside the box
 };
 
-// Damped-Jacobi sweep on the interior box I of a grain-map level (FP32): x_out = x + w (b - A x)/D
-// with A the interior row of Elastic<T>::Fapply.  gidm: grain id (low 16 bits) and the
+// One sweep over the interior box I of a grain-map level (FP32), A the interior row of
+// Elastic<T>::Fapply: OP = SPLIT_JACOBI, the damped-Jacobi update out = x + w (b - A x) / D
+// (Operator.cpp:109-157 as the FP32 cycle writes it); OP = SPLIT_RESIDUAL, out = b - A x (out may
+// alias b: each node reads its own b before writing).  gidm: grain id (low 16 bits) and the
 // directions with a non-zero grad C column (bits 16-18).  TABS: grain table in shared memory
 // (tab_n floats) or read through L1.  err: set when a TMA load did not complete.
-template <int M, bool TABS>
+enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1 };
+template <int M, bool TABS, int OP>
 __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
-    k_jacobi_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
+    k_sweep_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
                   const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_g, SCoef<float> K,
                   TileGeo T, int uniform, long long sy, long long sz, long long sc,
                   const unsigned* __restrict__ gidm_g, const float* __restrict__ tab, int tab_n, float* __restrict__ xo,
@@ -211,12 +218,13 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     auto load_v = [&](int k, unsigned bar) {
         const unsigned s = (unsigned)(k & 1);
         tma_load4(sb + 4u * (kOffB + s * SVS), &tm_b, xa, yv, k - T.slo[2], 0, bar);
-        tma_load4(sb + 4u * (kOffD + s * SVS), &tm_d, xa, yv, k - T.slo[2], 0, bar);
+        if (OP == SPLIT_JACOBI) tma_load4(sb + 4u * (kOffD + s * SVS), &tm_d, xa, yv, k - T.slo[2], 0, bar);
         tma_load4(sb + 4u * (kOffG + s * SVP), &tm_g, xa, yv, k - T.slo[2], 0, bar);
     };
+    constexpr unsigned kVTile = (OP == SPLIT_JACOBI ? 2 : 1) * kVBytes + kGBytes;
     // stage 0: planes k0-1, k0, k0+1 of x and the b, 1/D, id tiles of plane k0
     if (leader) {
-        mbar_expect_tx(bar0, 3 * kXBytes + 2 * kVBytes + kGBytes);
+        mbar_expect_tx(bar0, 3 * kXBytes + kVTile);
         load_x(k0 - 1, bar0);
         load_x(k0, bar0);
         load_x(k0 + 1, bar0);
@@ -237,7 +245,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             if (leader) {
                 const unsigned bn = bar0 + 8u * (unsigned)((s + 1) & 1);
                 asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                mbar_expect_tx(bn, kXBytes + 2 * kVBytes + kGBytes);
+                mbar_expect_tx(bn, kXBytes + kVTile);
                 load_x(k + 2, bn);
                 load_v(k + 1, bn);
             }
@@ -305,7 +313,10 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
         }
         if (act && !queued) {
 #pragma unroll
-            for (int n = 0; n < 3; ++n) xo[o + n * sc] = xv[n] + omega * (bv[n * SVP] - f[n]) * dv[n * SVP];
+            for (int n = 0; n < 3; ++n) {
+                if (OP == SPLIT_JACOBI) xo[o + n * sc] = xv[n] + omega * (bv[n * SVP] - f[n]) * dv[n * SVP];
+                else xo[o + n * sc] = bv[n * SVP] - f[n];
+            }
         }
         __syncthreads();
         // the queued nodes, one per thread: grad C columns of the directions whose neighbours lie in
@@ -350,7 +361,8 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             for (int r = 0; r < 3; ++r) {
                 float fr = qf[3 * e + r];
                 fr += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
-                xo[qo + r * sc] = qc[r * SXP] + omega * (qb[r * SVP] - fr) * qd[r * SVP];
+                if (OP == SPLIT_JACOBI) xo[qo + r * sc] = qc[r * SXP] + omega * (qb[r * SVP] - fr) * qd[r * SVP];
+                else xo[qo + r * sc] = qb[r * SVP] - fr;
             }
         }
         __syncthreads();
@@ -374,6 +386,25 @@ __global__ void __launch_bounds__(kBlock, 4)
     int i, j, k;
     unpack_node(list[t], S.lo, i, j, k);
     jacobi_node<M, float, true, SAME>(P, K, C, G, invD, D, xi, b, xo, omega, i, j, k);
+}
+
+// r = b - A x at the listed nodes (the per-node residual, k_residual's arithmetic); r may alias b
+template <int M>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_residual_list(OpParams P, SCoef<float> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
+                    View<const float> C, Grains<float> G, View<const float> x, View<const float> b, View<float> r) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_node(list[t], S.lo, i, j, k);
+    float v[3];
+    const long long ox = x.at(i, j, k);
+    apply_at<M, float, true>(P, K, C, G, x, i, j, k, ox, ox, v);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float rv = b.p[ox + q * x.sc] - v[q];
+        r.p[ox + q * x.sc] = rv;
+    }
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
@@ -413,14 +444,52 @@ CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUte
 
 size_t tile_smem(int tab_n, bool tabs) { return sizeof(float) * (size_t)(kOffT + (tabs ? tab_n : 0)); }
 
-template <int M, bool TABS>
+template <int M, bool TABS, int OP>
 void tile_smem_attr(size_t bytes) {
     static size_t set = 0;
     if (bytes > set) {
-        AE_CUDA_CHECK(cudaFuncSetAttribute(k_jacobi_tile<M, TABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        AE_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_tile<M, TABS, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes));
         set = bytes;
     }
+}
+
+// the tiled kernel of one operation over I; b: the right-hand side, invD: 1/D (Jacobi only)
+template <int OP>
+void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Box3& S, View<const float> x,
+                 const float* b, const float* invD, float* out, float omega, cudaStream_t st, Grains<float> G,
+                 int ngrains, int* err) {
+    const SCoef<float> K = make_scoef<float>(P.g);
+    dispatch_model<float>(P.model, [&](auto m) {
+        constexpr int Mv = decltype(m)::value;
+        TileGeo T;
+        T.I = I;
+        for (int q = 0; q < 3; ++q) T.slo[q] = S.lo[q];
+        const int nx = I.hi[0] - I.lo[0] + 1, ny = I.hi[1] - I.lo[1] + 1, nz = I.hi[2] - I.lo[2] + 1;
+        T.tiles_x = (nx + STX - 1) / STX;
+        const int tiles_y = (ny + STY - 1) / STY;
+        T.kz = sl.kz > 0 ? sl.kz : 8;
+        // every tile starts 32 nodes after the previous one, so one shift serves all of them
+        T.sh = (I.lo[0] - 1 - S.lo[0]) & 3;
+        const CUtensorMap tx = level_tmap(x.p, P.g, 3, SXR, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+        const CUtensorMap tb = level_tmap(b, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+        const CUtensorMap td = level_tmap(invD ? invD : b, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+        const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32);
+        const dim3 grid((unsigned)(T.tiles_x * tiles_y), (unsigned)((nz + T.kz - 1) / T.kz));
+        const int tab_n = ngrains * NCoef<Mv>::value;
+        const bool tabs = tab_n * (int)sizeof(float) <= kTabSmemMax;
+        const size_t smem = tile_smem(tab_n, tabs);
+        if (tabs) {
+            tile_smem_attr<Mv, true, OP>(smem);
+            k_sweep_tile<Mv, true, OP><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc,
+                                                                 sl.gidm, G.tab, tab_n, out, omega, err);
+        } else {
+            tile_smem_attr<Mv, false, OP>(smem);
+            k_sweep_tile<Mv, false, OP><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc,
+                                                                  sl.gidm, G.tab, tab_n, out, omega, err);
+        }
+        launched();
+    });
 }
 
 }  // namespace
@@ -439,75 +508,75 @@ bool split_supported(const Geo& g) {
     return true;
 }
 
+// count and fill the list of region R \ I (and, with gidm, the id/mask array)
+long long build_list(const Reg& reg, const Box3& R, const Box3& I, View<const unsigned short> gid, unsigned* gidm,
+                     unsigned long long** list, cudaStream_t st, unsigned long long* scratch_count) {
+    AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
+    k_split_mark<false><<<nblocks(reg.n), kBlock, 0, st>>>(reg, R, I, gid, nullptr, nullptr, scratch_count);
+    launched();
+    unsigned long long n = 0;
+    AE_CUDA_CHECK(cudaMemcpyAsync(&n, scratch_count, sizeof(n), cudaMemcpyDeviceToHost, st));
+    AE_CUDA_CHECK(cudaStreamSynchronize(st));
+    *list = nullptr;
+    if (n > 0) AE_CUDA_CHECK(cudaMalloc(list, sizeof(unsigned long long) * n));
+    if (n > 0 || gidm) {
+        AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
+        k_split_mark<true><<<nblocks(reg.n), kBlock, 0, st>>>(reg, R, I, gid, gidm, *list, scratch_count);
+        launched();
+        AE_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    return (long long)n;
+}
+
 long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& sl, cudaStream_t st,
                       unsigned long long* scratch_count) {
     if (!split_supported(g)) throw std::runtime_error("split sweep: level layout not supported");
     const Box3 S = geo_store(g);
     const Reg reg = make_reg(S);
     const Box3 I = split_interior(g);
-    AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
-    k_split_mark<false><<<nblocks(reg.n), kBlock, 0, st>>>(reg, I, gid, nullptr, nullptr, scratch_count);
-    launched();
-    unsigned long long n = 0;
-    AE_CUDA_CHECK(cudaMemcpyAsync(&n, scratch_count, sizeof(n), cudaMemcpyDeviceToHost, st));
-    AE_CUDA_CHECK(cudaStreamSynchronize(st));
     AE_CUDA_CHECK(cudaMalloc(&sl.gidm, sizeof(unsigned) * (size_t)geo_nn(g)));
     AE_CUDA_CHECK(cudaMemsetAsync(sl.gidm, 0, sizeof(unsigned) * (size_t)geo_nn(g), st));
-    if (n > 0) AE_CUDA_CHECK(cudaMalloc(&sl.list, sizeof(unsigned long long) * n));
-    AE_CUDA_CHECK(cudaMemsetAsync(scratch_count, 0, sizeof(unsigned long long), st));
-    k_split_mark<true><<<nblocks(reg.n), kBlock, 0, st>>>(reg, I, gid, sl.gidm, sl.list, scratch_count);
-    launched();
-    AE_CUDA_CHECK(cudaStreamSynchronize(st));
-    sl.n = (long long)n;
+    // the Jacobi sweep writes the whole storage box, the residual the apply region
+    sl.n = build_list(reg, S, I, gid, sl.gidm, &sl.list, st, scratch_count);
+    sl.n_r = build_list(reg, geo_apply_region(g), I, gid, nullptr, &sl.list_r, st, scratch_count);
     return sl.n;
 }
 
 void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
                          View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
                          cudaStream_t st, Grains<float> G, int ngrains, int* err) {
-    const SCoef<float> K = make_scoef<float>(P.g);
     const Box3 S = geo_store(P.g);
     const Box3 I = split_interior(P.g);
     const bool same = same_layout(xi, C) && same_layout(xi, invD) && same_layout(xi, D) && same_layout(xi, b) &&
                       same_layout(xi, xo);
     if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
-    dispatch_model<float>(P.model, [&](auto m) {
-        constexpr int Mv = decltype(m)::value;
-        if (!box_empty(I)) {
-            TileGeo T;
-            T.I = I;
-            for (int q = 0; q < 3; ++q) T.slo[q] = S.lo[q];
-            const int nx = I.hi[0] - I.lo[0] + 1, ny = I.hi[1] - I.lo[1] + 1, nz = I.hi[2] - I.lo[2] + 1;
-            T.tiles_x = (nx + STX - 1) / STX;
-            const int tiles_y = (ny + STY - 1) / STY;
-            T.kz = sl.kz > 0 ? sl.kz : 16;
-            // every tile starts 32 nodes after the previous one, so one shift serves all of them
-            T.sh = (I.lo[0] - 1 - S.lo[0]) & 3;
-            const CUtensorMap tx = level_tmap(xi.p, P.g, 3, SXR, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-            const CUtensorMap tb = level_tmap(b.p, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-            const CUtensorMap td = level_tmap(invD.p, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-            const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32);
-            const dim3 grid((unsigned)(T.tiles_x * tiles_y), (unsigned)((nz + T.kz - 1) / T.kz));
-            const int tab_n = ngrains * NCoef<Mv>::value;
-            const bool tabs = tab_n * (int)sizeof(float) <= kTabSmemMax;
-            const size_t smem = tile_smem(tab_n, tabs);
-            if (tabs) {
-                tile_smem_attr<Mv, true>(smem);
-                k_jacobi_tile<Mv, true><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, xi.sy, xi.sz, xi.sc,
-                                                                  sl.gidm, G.tab, tab_n, xo.p, omega, err);
-            } else {
-                tile_smem_attr<Mv, false>(smem);
-                k_jacobi_tile<Mv, false><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, xi.sy, xi.sz,
-                                                                   xi.sc, sl.gidm, G.tab, tab_n, xo.p, omega, err);
-            }
-            launched();
-        }
-        if (sl.n > 0) {
-            k_jacobi_list<Mv, true><<<(unsigned)((sl.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+    if (!box_empty(I)) launch_tile<SPLIT_JACOBI>(P, sl, I, S, xi, b.p, invD.p, xo.p, omega, st, G, ngrains, err);
+    if (sl.n > 0) {
+        const SCoef<float> K = make_scoef<float>(P.g);
+        dispatch_model<float>(P.model, [&](auto m) {
+            k_jacobi_list<decltype(m)::value, true><<<(unsigned)((sl.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(
                 P, K, sl.list, sl.n, S, C, G, invD, D, xi, b, xo, omega);
-            launched();
-        }
-    });
+        });
+        launched();
+    }
+}
+
+void launch_residual_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> x,
+                           View<const float> b, View<float> r, cudaStream_t st, Grains<float> G, int ngrains,
+                           int* err) {
+    const Box3 S = geo_store(P.g);
+    const Box3 I = split_interior(P.g);
+    const bool same = same_layout(x, C) && same_layout(x, b) && same_layout(x, r);
+    if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
+    if (!box_empty(I)) launch_tile<SPLIT_RESIDUAL>(P, sl, I, S, x, b.p, nullptr, r.p, 0.0f, st, G, ngrains, err);
+    if (sl.n_r > 0) {
+        const SCoef<float> K = make_scoef<float>(P.g);
+        dispatch_model<float>(P.model, [&](auto m) {
+            k_residual_list<decltype(m)::value><<<(unsigned)((sl.n_r + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+                P, K, sl.list_r, sl.n_r, S, C, G, x, b, r);
+        });
+        launched();
+    }
 }
 
 }  // namespace ae

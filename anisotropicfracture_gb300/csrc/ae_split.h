@@ -11,8 +11,10 @@ struct SplitList {
     unsigned long long* list = nullptr;  // nodes outside the interior box: packed offsets from the
                                          // storage box's low corner
     long long n = 0;
+    unsigned long long* list_r = nullptr;  // the same for the residual's region grow(valid,1) ∩ domain
+    long long n_r = 0;
     unsigned* gidm = nullptr;            // per stored node: grain id | grad C directions << 16
-    int kz = 0;                          // planes per block of the tiled kernel (0: default 16)
+    int kz = 0;                          // planes per block of the tiled kernel (0: default 8)
 };
 // grain ids the split sweep can carry next to its 3-bit direction mask
 constexpr int kSplitMaxGrains = 1 << 16;
@@ -32,5 +34,9 @@ long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& s
 void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
                          View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
                          cudaStream_t st, Grains<float> G, int ngrains, int* err);
+// r = b - A x (FP32) on the apply region of a grain-map level, the same split; r may alias b.
+void launch_residual_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> x,
+                           View<const float> b, View<float> r, cudaStream_t st, Grains<float> G, int ngrains,
+                           int* err);
 
 }  // namespace ae
