@@ -35,7 +35,7 @@ class SolverOpts(C.Structure):
     _fields_ = [("max_fmg_iter", C.c_int), ("nu1", C.c_int), ("nu2", C.c_int), ("sweeps", C.c_int), ("bottom", C.c_int),
                 ("max_iter", C.c_int), ("bottom_max_iter", C.c_int), ("bottom_reltol", C.c_double),
                 ("nuf", C.c_int), ("max_mg_levels", C.c_int), ("omega", C.c_double), ("precision", C.c_int),
-                ("inner_cycles", C.c_int), ("verbose", C.c_int), ("use_graph", C.c_int)]
+                ("inner_cycles", C.c_int), ("verbose", C.c_int), ("use_graph", C.c_int), ("fixed_iter", C.c_int)]
 
 
 class SolveStats(C.Structure):

@@ -837,7 +837,9 @@ void solve_ml(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs
         }
     };
     try {
-        while (!conv && iters < o.max_iter) {
+        // MLMG with fixed_iter: exactly that many iterations, whatever the residual
+        const bool fixed = o.fixed_iter > 0;
+        while (fixed ? iters < o.fixed_iter : (!conv && iters < o.max_iter)) {
             const bool fcyc = iters < o.max_fmg_iter;
             const int q = fcyc ? 0 : 1;
             if (o.use_graph && !exec[q]) {
@@ -888,7 +890,7 @@ void solve_ml(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs
         stats->resfinal = rn;
         stats->target = target;
     }
-    if (!conv) throw ApiErr(AE_ERR_NOT_CONVERGED, "MLMG failed to converge within max_iter");
+    if (!conv && o.fixed_iter <= 0) throw ApiErr(AE_ERR_NOT_CONVERGED, "MLMG failed to converge within max_iter");
 }
 
 }  // namespace
@@ -917,6 +919,7 @@ void ae_default_solver_opts(ae_solver_opts* o) {
     o->inner_cycles = 1;
     o->verbose = 0;
     o->use_graph = 1;
+    o->fixed_iter = 0;
 }
 
 int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) {

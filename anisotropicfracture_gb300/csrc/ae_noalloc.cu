@@ -58,12 +58,13 @@ extern "C" int ae_bottom_solve_noalloc(const ae_level_desc* level, int model, co
         g.vlo[d] = 0;
         g.vhi[d] = level->domain_cells[d];
         g.dx[d] = level->dx[d];
+        // checked after every factor, so the product cannot overflow before the test
         nn *= (long long)level->domain_cells[d] + 1;
+        if (level->domain_cells[d] >= AE_NOALLOC_MAX_NODES || nn > AE_NOALLOC_MAX_NODES)
+            return fail(AE_ERR_ARG, "level too large: ae_bottom_solve_noalloc handles at most " +
+                                        std::to_string(AE_NOALLOC_MAX_NODES) + " nodes (its fixed work space)");
     }
     g.ng = 0;
-    if (nn > AE_NOALLOC_MAX_NODES)
-        return fail(AE_ERR_ARG, "level has " + std::to_string(nn) + " nodes; ae_bottom_solve_noalloc handles at most " +
-                                    std::to_string(AE_NOALLOC_MAX_NODES) + " (its fixed work space)");
     OpParams P;
     P.g = g;
     P.model = model;

@@ -311,6 +311,10 @@ class Linear:
     def setMaxFmgIter(self, n):
         self.opts.max_fmg_iter = int(min(n, 2 ** 31 - 1))
 
+    def setFixedIter(self, n):
+        """Run exactly n iterations, converged or not (MLMG fixed_iter)."""
+        self.opts.fixed_iter = int(n)
+
     def setBottomSolver(self, name):
         self.opts.bottom = {"cg": 0, "bicgstab": 1}[name]
 
@@ -349,6 +353,8 @@ class Linear:
             value.setBottomMaxIter(int(pp["bottom_max_iter"]))
         if "max_fmg_iter" in pp:
             value.setMaxFmgIter(int(pp["max_fmg_iter"]))
+        if "fixed_iter" in pp:
+            value.setFixedIter(int(pp["fixed_iter"]))
         if "verbose" in pp:
             value.setVerbose(int(pp["verbose"]))
         if "bottom_solver" in pp:

@@ -97,6 +97,9 @@ typedef struct {
     int inner_cycles;     /* precision 1: FP32 cycles per FP64 residual                       */
     int verbose;
     int use_graph;        /* capture each iteration in a CUDA graph                           */
+    int fixed_iter;       /* > 0: run exactly this many iterations, converged or not (MLMG     
+                             fixed_iter, Solver::Nonlocal::Linear::Parse "fixed_iter",
+                             src/Solver/Nonlocal/Linear.H:132-133); 0: iterate to the tolerance */
 } ae_solver_opts;
 
 typedef struct {
@@ -244,7 +247,12 @@ long long ae_op_device_bytes(const ae_op* op);
  *  - bctype: host array [26][3] of ae_bc_type.  *krylov_failed (may be NULL) receives the
  *    number of failed Krylov solves (0 or 1).
  *  - The first call on a device looks up the work space's device address with that device
- *    current; make that first call before any stream capture.
+ *    current; make that first call before any stream capture.  With CUDA's lazy module loading
+ *    that first call also loads the library's device code, which can itself need device memory
+ *    from the driver: make it (or run with CUDA_MODULE_LOADING=EAGER) before the application's
+ *    arena reserves the device.
+ *  - The address is kept per device for the life of the process; after a cudaDeviceReset the
+ *    kept address is stale, so the entry point must not be called again in that process.
  *  - Every call shares the one work space: calls that overlap on the GPU (other streams, other
  *    host threads) race.  The call synchronizes `stream` (a cudaStream_t) before returning. */
 #define AE_NOALLOC_MAX_NODES 4913 /* 17^3 */

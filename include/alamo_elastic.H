@@ -319,6 +319,7 @@ public:
     void setMaxIter(int n) { m_opts.max_iter = n; }
     void setBottomMaxIter(int n) { m_opts.bottom_max_iter = n; }
     void setMaxFmgIter(int n) { m_opts.max_fmg_iter = n; }
+    void setFixedIter(int n) { m_opts.fixed_iter = n; }
     void setVerbose(int v) { m_opts.verbose = v; }
     void setBottomSolverCG(bool cg) { m_opts.bottom = cg ? 0 : 1; }
     void setPreSmooth(int n) { m_opts.nu1 = n; }

@@ -172,3 +172,21 @@ def test_error_behaviour():
     with pytest.raises(AeError) as e:
         op3.prepareForSolve()
     assert e.value.code == _lib.AE_ERR_NAN
+
+
+def test_fixed_iter_runs_exactly_that_many_iterations():
+    """MLMG fixed_iter (Solver::Nonlocal::Linear::Parse, Linear.H:132-133): the solve stops after
+    exactly that many iterations and reports no convergence failure; the iterate equals the one an
+    ordinary solve has after as many iterations."""
+    n = 16
+    L, Cf, bc, b = sphere_inclusion_problem(n)
+    op, s = gpu_solver(n, models.ISOTROPIC, Cf, bc)
+    s.setFixedIter(3)
+    x = np.zeros_like(b)
+    s.solve(Field(x), Field(b), 1e-14, 0.0)
+    assert s.stats.iters == 3 and not s.stats.converged
+    op2, s2 = gpu_solver(n, models.ISOTROPIC, Cf, bc, max_iter=3)
+    x2 = np.zeros_like(b)
+    with pytest.raises(AeError):
+        s2.solve(Field(x2), Field(b), 1e-14, 0.0)
+    assert np.array_equal(x, x2)

@@ -11,6 +11,9 @@ def test_linear_defaults_and_keys():
     o = s.opts
     assert (o.max_iter, o.bottom_max_iter, o.max_fmg_iter, o.verbose, o.bottom, o.nu1, o.nu2) == (50, 20, 0, 2, 0, 3, 4)
     assert s.m_tol_rel == 1e-9
+    assert o.fixed_iter == 0
+    Linear.Parse(s, {"fixed_iter": "6"})  # Linear.H:132-133
+    assert s.opts.fixed_iter == 6
 
 
 def test_newton_adds_nriters():
