@@ -107,6 +107,8 @@ SIGNATURES = {
     "ae_newton_residual": ([P, C.c_int, FAB, FAB, FAB, FAB], C.c_int),
     "ae_newton_dw": ([P, C.c_int, FAB, FAB, FAB, FAB], C.c_int),
     "ae_solve": ([P, FAB, FAB, C.c_double, C.c_double, C.POINTER(SolverOpts), C.POINTER(SolveStats)], C.c_int),
+    "ae_solveaffine": ([P, FAB, FAB, C.c_double, C.c_double, C.c_int, C.POINTER(SolverOpts), C.POINTER(SolveStats)],
+                       C.c_int),
     "ae_bottom_solve_noalloc": ([C.POINTER(LevelDesc), C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p,
                                  C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), C.c_void_p],
                                 C.c_int),

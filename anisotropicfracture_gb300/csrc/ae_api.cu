@@ -1523,8 +1523,9 @@ int ae_energy(ae_op* op, int amrlev, const ae_fab* w, const ae_fab* u) {
     });
 }
 
-int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
-             const ae_solver_opts* opts, ae_solve_stats* stats) {
+// ae_solve and ae_solveaffine: affine < 0 plain solve; 0 / 1 solveaffine without / with copyrhs
+static int solve_entry(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
+                const ae_solver_opts* opts, ae_solve_stats* stats, int affine) {
     return guarded([&] {
         const auto t0 = std::chrono::steady_clock::now();
         require(op != nullptr && sol != nullptr && rhs != nullptr, "null argument");
@@ -1551,6 +1552,46 @@ int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, do
             const Geo& g = A.mg[0].g;
             launch_copy<double, double>(region[a], 3, level_view(g, A.rhs), device_view_in(op, rhs[a], 0), op->st);
             launch_copy<double, double>(region[a], 3, level_view(g, A.sol), device_view_in(op, sol[a], 1), op->st);
+        }
+        if (affine >= 0) {
+            // Solver::Nonlocal::Linear::solveaffine (src/Solver/Nonlocal/Linear.H:41-100):
+            // rhs_tmp = MLMG::apply(0) with the inhomogeneous operator (composite: each level's
+            // apply, the finer level's restricted onto the coarse nodes it covers), then -rhs_tmp
+            // inside the domain and 0 on its boundary, added to rhs; the solve is homogeneous.
+            // AmrIter::ml_residual with x = b = 0 gives r = -rhs_tmp.
+            op->homogeneous = 0;
+            std::vector<double*> zx, zb;
+            for (int a = 0; a < namr; ++a) {
+                MGLevel& L = op->amr[a].mg[0];
+                launch_fill<double>(geo_store(L.g), 3, level_view(L.g, L.tmp), 0.0, op->st);
+                launch_fill<double>(geo_store(L.g), 3, level_view(L.g, L.corhold), 0.0, op->st);
+                zx.push_back(L.tmp);
+                zb.push_back(L.corhold);
+            }
+            AmrIter<double> it{op, o, op->st, zx, zb};
+            it.ml_residual();
+            for (int a = 0; a < namr; ++a) {
+                AmrLevel& A = op->amr[a];
+                const Geo& g = A.mg[0].g;
+                launch_affine_rhs(g, region[a], level_view(g, A.rhs), cview(level_view(g, A.mg[0].res)), op->st);
+                if (affine == 1) {  // copyrhs: the caller's rhs receives the modified right-hand side
+                    if (is_device_ptr(rhs[a].data)) {
+                        launch_copy<double, double>(region[a], 3, fab_view<double>(rhs[a]), cview(level_view(g, A.rhs)),
+                                                    op->st);
+                    } else {
+                        const size_t bytes = sizeof(double) * (size_t)fab_elems(rhs[a]);
+                        ensure_stage(op->stage2, op->stage2_bytes, bytes);
+                        ae_fab d = rhs[a];
+                        d.data = op->stage2;
+                        AE_CHECK(cudaMemcpyAsync(op->stage2, rhs[a].data, bytes, cudaMemcpyHostToDevice, op->st));
+                        launch_copy<double, double>(region[a], 3, fab_view<double>(d), cview(level_view(g, A.rhs)),
+                                                    op->st);
+                        AE_CHECK(cudaMemcpyAsync(rhs[a].data, op->stage2, bytes, cudaMemcpyDeviceToHost, op->st));
+                        AE_CHECK(cudaStreamSynchronize(op->st));
+                    }
+                }
+            }
+            op->homogeneous = 1;
         }
         int status = AE_OK;
         std::string msg;
@@ -1585,6 +1626,16 @@ int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, do
         if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (status != AE_OK) throw ApiErr(status, msg);
     });
+}
+
+int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
+             const ae_solver_opts* opts, ae_solve_stats* stats) {
+    return solve_entry(op, sol, rhs, tol_rel, tol_abs, opts, stats, -1);
+}
+
+int ae_solveaffine(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs, int copyrhs,
+                   const ae_solver_opts* opts, ae_solve_stats* stats) {
+    return solve_entry(op, sol, rhs, tol_rel, tol_abs, opts, stats, copyrhs ? 1 : 0);
 }
 
 long long ae_kernel_launches(void) { return g_kernel_launches.load(); }

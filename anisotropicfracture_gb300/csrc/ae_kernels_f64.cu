@@ -702,4 +702,23 @@ void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st)
     launched();
 }
 
+// Linear::solveaffine's right-hand side (src/Solver/Nonlocal/Linear.H:62-89): with r = 0 - A 0,
+// the negated apply of zero, rhs += r on nodes inside the domain, nothing on its boundary.
+__global__ void __launch_bounds__(kBlock) k_affine_rhs(Geo g, Reg reg, View<double> rhs, View<const double> r) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    if (i == g.dlo[0] || i == g.dhi[0] || j == g.dlo[1] || j == g.dhi[1] || k == g.dlo[2] || k == g.dhi[2]) return;
+    const long long o = rhs.at(i, j, k), q = r.at(i, j, k);
+#pragma unroll
+    for (int n = 0; n < 3; ++n) rhs.p[o + n * rhs.sc] += r.p[q + n * r.sc];
+}
+void launch_affine_rhs(const Geo& g, const Box3& region, View<double> rhs, View<const double> r, cudaStream_t st) {
+    const Reg reg = make_reg(region);
+    if (reg.n == 0) return;
+    k_affine_rhs<<<nblocks(reg.n), kBlock, 0, st>>>(g, reg, rhs, r);
+    launched();
+}
+
 }  // namespace ae

@@ -155,6 +155,8 @@ void launch_norminf(const Box3& region, int ncomp, View<const R> v, unsigned lon
 void launch_bc_init(const Geo& g, const BCP& bc, const double* val, int homogeneous, View<double> rhs,
                     cudaStream_t st);
 void launch_strain(const Geo& g, View<const double> u, View<double> e, int voigt, cudaStream_t st);
+// rhs += r on the nodes of region not on the domain boundary (Linear::solveaffine)
+void launch_affine_rhs(const Geo& g, const Box3& region, View<double> rhs, View<const double> r, cudaStream_t st);
 void launch_stress(const OpParams& P, View<const double> C, View<const double> u, View<double> s, int voigt,
                    cudaStream_t st);
 void launch_energy(const OpParams& P, View<const double> C, View<const double> u, View<double> w, cudaStream_t st);

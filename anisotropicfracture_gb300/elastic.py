@@ -344,6 +344,20 @@ class Linear:
                               C.byref(self.stats)))
         return self.stats.resfinal
 
+    def solveaffine(self, sol, rhs, tol_rel=None, tol_abs=None, copyrhs=False):
+        """Linear::solveaffine (src/Solver/Nonlocal/Linear.H:41-100): rhs plus the negated apply of
+        zero by the inhomogeneous operator (zero on the domain boundary), solved homogeneously;
+        copyrhs writes that right-hand side back into rhs.  Returns the final residual max-norm."""
+        sol = sol if isinstance(sol, (list, tuple)) else [sol]
+        rhs = rhs if isinstance(rhs, (list, tuple)) else [rhs]
+        fs = (Fab * len(sol))(*[s.fab() for s in sol])
+        fr = (Fab * len(rhs))(*[r.fab() for r in rhs])
+        tr = self.m_tol_rel if tol_rel is None else tol_rel
+        ta = self.m_tol_abs if tol_abs is None else tol_abs
+        check(load().ae_solveaffine(self.linop.handle, fs, fr, float(tr), float(ta), int(bool(copyrhs)),
+                                    C.byref(self.opts), C.byref(self.stats)))
+        return self.stats.resfinal
+
     @staticmethod
     def Parse(value, pp):
         """Keys of src/Solver/Nonlocal/Linear.H:121-140 plus bottom_solver, precision, pre/post smooth."""

@@ -217,6 +217,13 @@ int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fa
  * Returns AE_ERR_NOT_CONVERGED if max_iter is reached. */
 int ae_solve(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs,
              const ae_solver_opts* opts, ae_solve_stats* stats);
+/* Solver::Nonlocal::Linear::solveaffine (src/Solver/Nonlocal/Linear.H:41-100): the operator with
+ * its inhomogeneous rows is applied to zero (MLMG::apply), the result is negated inside the domain
+ * and zeroed on its boundary and added to rhs (written back to rhs when copyrhs != 0), and the
+ * homogeneous operator solves for that right-hand side.  Arguments and returns as ae_solve.  For
+ * the linear stiffness kinds the apply of zero is exactly zero, so the solve sees rhs itself. */
+int ae_solveaffine(ae_op* op, const ae_fab* sol, const ae_fab* rhs, double tol_rel, double tol_abs, int copyrhs,
+                   const ae_solver_opts* opts, ae_solve_stats* stats);
 
 /* The nodal plotfile of Integrator::WritePlotFile (src/Integrator/Integrator.cpp:582-681, the
  * "node" half, written by amrex::WriteMultiLevelPlotfile): an AMReX plotfile directory

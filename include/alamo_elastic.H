@@ -334,6 +334,16 @@ public:
         return m_stats.resfinal;
     }
     double solve(std::vector<alamo::Fab>& sol, std::vector<alamo::Fab>& rhs) { return solve(sol, rhs, m_tol_rel, m_tol_abs); }
+    // Linear::solveaffine(sol, rhs, tol_rel, tol_abs, copyrhs) (Linear.H:41-100)
+    double solveaffine(std::vector<alamo::Fab>& sol, std::vector<alamo::Fab>& rhs, double tol_rel, double tol_abs,
+                       bool copyrhs = false) {
+        std::vector<ae_fab> s, r;
+        for (auto& f : sol) s.push_back(f.c());
+        for (auto& f : rhs) r.push_back(f.c());
+        alamo::check(ae_solveaffine(linop.handle(), s.data(), r.data(), tol_rel, tol_abs, copyrhs ? 1 : 0, &m_opts,
+                                    &m_stats));
+        return m_stats.resfinal;
+    }
     const ae_solve_stats& stats() const { return m_stats; }
 
 protected:

@@ -190,3 +190,38 @@ def test_fixed_iter_runs_exactly_that_many_iterations():
     with pytest.raises(AeError):
         s2.solve(Field(x2), Field(b), 1e-14, 0.0)
     assert np.array_equal(x, x2)
+
+
+@pytest.mark.parametrize("nlev", [1, 2])
+def test_solveaffine_equals_solve_for_linear_models(nlev):
+    """Linear::solveaffine (Linear.H:41-100) adds the negated apply of zero by the inhomogeneous
+    operator to rhs inside the domain.  For the linear stiffness kinds that apply is exactly zero:
+    the solution equals Linear::solve's bit for bit, and copyrhs writes back rhs unchanged."""
+    from helpers import polycrystal_amr
+    Ls, Cs, bc, bs = polycrystal_amr(16, nlev)
+    lo = [tuple(L.lo[d] - L.ng for d in range(3)) for L in Ls]
+    descs = [level_desc(tuple(L.dom_hi[d] for d in range(3)), lo=tuple(L.lo), hi=tuple(L.hi), dx=tuple(L.dx))
+             for L in Ls]
+    out = []
+    for affine in (False, True):
+        op = Elastic(descs, models.MAJORMINOR)
+        for a in range(nlev):
+            op.SetModel(a, Field(Cs[a], lo[a]))
+        op.SetBC(bc)
+        op.SetUniform(False)
+        s = Linear(op)
+        s.setMaxFmgIter(0)
+        xs = [np.zeros_like(b) for b in bs]
+        rs = [b.copy() for b in bs]
+        fx = [Field(x, l) for x, l in zip(xs, lo)]
+        fr = [Field(r, l) for r, l in zip(rs, lo)]
+        if affine:
+            s.solveaffine(fx, fr, 1e-8, 0.0, copyrhs=True)
+            for r, b in zip(rs, bs):
+                assert np.array_equal(r, b)
+        else:
+            s.solve(fx, fr, 1e-8, 0.0)
+        out.append((s.stats.iters, xs))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
