@@ -785,19 +785,22 @@ def cells_oracle_check(work, sols, nsample):
     return out
 
 
-def serve_run(work, rate, precision, inner, seed=7):
-    """Poisson arrivals at `rate` requests/s into a fresh server."""
+def serve_run(work, rate, precision, inner, seed=7, rank=0, world=1):
+    """Poisson arrivals at `rate` requests/s into a fresh server.  With world > 1 this rank's server
+    takes the requests i = rank (mod world) of the stream, at their times in the whole stream."""
     from anisotropicfracture_gb300 import cells, models
     S = cells.CellServer(models.MAJORMINOR, precision=precision, inner_cycles=inner, **CELL_SOLVER)
     loads = cells.unit_strains()
-    gaps = np.random.default_rng(seed).exponential(1.0 / rate, size=len(work))
+    times = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, size=len(work)))
+    mine = list(range(rank, len(work), world))
+    work = [work[i] for i in mine]
+    offsets = [float(times[i]) for i in mine]
     tickets = []
 
     def producer():
-        t_next = time.perf_counter()
-        for w, g in zip(work, gaps):
-            t_next += g
-            dt = t_next - time.perf_counter()
+        t0 = time.perf_counter()
+        for w, t in zip(work, offsets):
+            dt = t0 + t - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
             tickets.append(S.submit(w["n"], loads, w["seeds"], w["table"]))
@@ -828,7 +831,8 @@ def serve_run(work, rate, precision, inner, seed=7):
     def pct(a, q):
         return float(np.percentile(a, q))
 
-    return {"rate": rate, "requests": len(work), "ok": len(good) == len(res),
+    return {"rate": rate, "requests": len(work), "ok": len(good) == len(res), "lat": lat.tolist(),
+            "queue": queue.tolist(), "service": service.tolist(), "solves": nsolves,
             "offered_solves_per_s": rate * len(cells.unit_strains()),
             "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
             "queue_p50_s": pct(queue, 50), "queue_p99_s": pct(queue, 99),
@@ -837,12 +841,44 @@ def serve_run(work, rate, precision, inner, seed=7):
             "solves_per_s": nsolves / (last - first), "iterations": st["iterations"], "busy_s": st["busy_seconds"]}
 
 
-def bench_serve(args):
+def _serve_over_ranks(work, rate, precision, inner, rank, world):
+    """One arrival rate: every rank serves its share of the stream; rank 0 merges the records
+    (latency percentiles over all requests, solves/s summed over the concurrently serving ranks)."""
+    _barrier(world)
+    r = serve_run(work, rate, precision, inner, rank=rank, world=world)
+    if world > 1:
+        import torch.distributed as dist
+        parts = [None] * world
+        dist.all_gather_object(parts, r)
+    else:
+        parts = [r]
+    lat = np.concatenate([p["lat"] for p in parts])
+    queue = np.concatenate([p["queue"] for p in parts])
+    service = np.concatenate([p["service"] for p in parts])
+
+    def pct(a, q):
+        return float(np.percentile(a, q))
+
+    out = {"rate": rate, "requests": int(lat.size), "ok": all(p["ok"] for p in parts),
+           "offered_solves_per_s": parts[0]["offered_solves_per_s"],
+           "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "queue_p50_s": pct(queue, 50), "queue_p99_s": pct(queue, 99),
+           "service_p50_s": pct(service, 50), "service_p99_s": pct(service, 99),
+           "resident_mean": float(sum(p["resident_mean"] for p in parts)),
+           "resident_max": int(sum(p["resident_max"] for p in parts)),
+           "solves_per_s": float(sum(p["solves_per_s"] for p in parts)),
+           "iterations": int(max(p["iterations"] for p in parts)), "busy_s": float(max(p["busy_s"] for p in parts))}
+    if world > 1:
+        out["ranks"] = world
+    return out
+
+
+def bench_serve(args, rank=0, world=1):
     """Served cells: for each arrival rate a fresh server takes a Poisson stream of requests.
     Latency (submission to result) is split into queueing delay (submission to admission) and
     service time (admission to result); `resident_*` counts requests on the device at once.
     The sub-capacity rates show overlap below saturation; above capacity the queue grows and
-    latency measures the backlog."""
+    latency measures the backlog.  With N ranks each GPU serves every N-th request of the stream
+    (no exchange between the servers) and solves/s adds up over the ranks."""
     rates = [float(r) for r in args.serve_rates.split(",") if r]
     rates64 = [float(r) for r in args.serve_fp64_rates.split(",") if r]
     work = serve_workload(max(args.serve_requests, args.serve_fp64_requests))
@@ -850,11 +886,12 @@ def bench_serve(args):
                        "8-64 grains, 6 unit strains (1e-3) per request, tol_rel 1e-8",
            "requests_per_rate": {"mixed": args.serve_requests, "fp64": args.serve_fp64_requests},
            "mean_nodes": float(np.mean([w["n"] ** 3 for w in work[:args.serve_requests]])),
-           "inner_cycles": args.batch_inner, "unit": UNIT}
+           "inner_cycles": args.batch_inner, "unit": UNIT, "ranks": world}
     # warm-up: one small request (library load, first graph capture)
     serve_run(work[:1], 1000.0, 1, args.batch_inner)
-    out["mixed"] = [serve_run(work[:args.serve_requests], r, 1, args.batch_inner) for r in rates]
-    out["fp64"] = [serve_run(work[:args.serve_fp64_requests], r, 0, args.batch_inner) for r in rates64]
+    out["mixed"] = [_serve_over_ranks(work[:args.serve_requests], r, 1, args.batch_inner, rank, world) for r in rates]
+    out["fp64"] = [_serve_over_ranks(work[:args.serve_fp64_requests], r, 0, args.batch_inner, rank, world)
+                   for r in rates64]
     cap_m = max(r["solves_per_s"] for r in out["mixed"])
     cap_f = max(r["solves_per_s"] for r in out["fp64"])
     out["capacity_solves_per_s"] = {"mixed": cap_m, "fp64": cap_f,
@@ -881,6 +918,8 @@ def main():
     ap.add_argument("--mixed-tight-tol", type=float, default=0.0,
                     help="also time the mixed solve to this residual and report its error (0: off)")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--bicgstab-steps", type=int, default=1,
+                    help="timed mixed solves with the BiCGStab bottom solver (0: off)")
     ap.add_argument("--ref-sample-iters", type=int, default=3,
                     help="composite oracle iterations per step of the reference arm")
     ap.add_argument("--cpu-sample-iters", type=int, default=1)
@@ -919,6 +958,16 @@ def main():
     ap.add_argument("--serve-fp64-rates", default="1,50", help="arrival rates (requests/s), FP64")
     args = ap.parse_args()
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N outside a launcher: start N ranks, one per GPU, as torchrun would
+        import socket
+        sk = socket.socket()
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+        sk.close()
+        os.execvp(sys.executable, [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                                   "--nproc-per-node", str(args.gpus), "--master-addr", "127.0.0.1",
+                                   "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:])
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -1125,6 +1174,19 @@ def main():
                                      "ms_per_solve": ms_t, "iters": st_t.iters, "converged": bool(st_t.converged),
                                      "displacement_err": err_vs_oracle([x.cpu().numpy() for x in sol_d])}
 
+    # the same mixed solve with the reference's default bottom solver (BiCGStab, Linear.H:25): CG
+    # fails on the non-symmetric coarsest operator every call and falls back to smoothing
+    bicg = None
+    if args.bicgstab_steps > 0:
+        solver.setBottomSolver("bicgstab")
+        solve_device("mixed")
+        ms_b, st_b = timed("mixed", args.bicgstab_steps)
+        bicg = {"value": world * 1000.0 / ms_b, "unit": UNIT, "ms_per_solve": ms_b, "iters": st_b.iters,
+                "bottom_failures": st_b.bottom_fail, "converged": bool(st_b.converged),
+                "cycle": "V-cycle, 2 pre + 2 post damped-Jacobi sweeps, BiCGStab bottom"}
+        solver.setBottomSolver("cg")
+    bottom_fail_cg = st_mixed.bottom_fail
+
     # end to end through the C ABI with pinned host buffers
     solver.setPrecision("mixed")
     rhs_p = [torch.from_numpy(b).pin_memory() for b in rhs_h]
@@ -1197,6 +1259,8 @@ def main():
         "mixed_over_fp64": (ms_fp64 / ms_mixed) if ms_fp64 else None,
         "displacement_err_mixed_vs_fp64": disp_err,
         "fp64_oracle": oracle,
+        "bottom_failures_cg": bottom_fail_cg,
+        "mixed_bicgstab_bottom": bicg,
         "oracle_check": checks,
         "parity_at_size": parity,
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -1231,13 +1295,21 @@ def main():
 
 
 def add_cell_workloads(args, lib, line, rank, world):
-    """The damaged-polycrystal, batched and served cell workloads.  The batch shards over ranks;
-    the single-box damaged solve and the server (one request loop per GPU) run on a 1-GPU job."""
+    """The damaged-polycrystal, batched and served cell workloads.  The batch and the served stream
+    shard over ranks (cells / requests, no data-path exchange); the single-box damaged solve and
+    the model builders run on a 1-GPU job."""
     if not args.no_batch:
         try:
             line["batch"] = bench_batch(args, lib, rank, world)
         except Exception as e:  # pragma: no cover
             line["batch"] = {"error": str(e)}
+    if not args.no_serve:
+        try:
+            sv = bench_serve(args, rank, world)
+            if rank == 0:
+                line["serve"] = sv
+        except Exception as e:  # pragma: no cover
+            line["serve"] = {"error": str(e)}
     if world > 1 or rank != 0:
         return
     if not args.no_damaged:
@@ -1245,11 +1317,6 @@ def add_cell_workloads(args, lib, line, rank, world):
             line["damaged_polycrystal"] = bench_damaged_polycrystal(args)
         except Exception as e:  # pragma: no cover
             line["damaged_polycrystal"] = {"error": str(e)}
-    if not args.no_serve:
-        try:
-            line["serve"] = bench_serve(args)
-        except Exception as e:  # pragma: no cover
-            line["serve"] = {"error": str(e)}
     if not args.no_builders:
         try:
             line["model_builders"] = bench_model_builders(args)

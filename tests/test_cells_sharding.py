@@ -1,9 +1,11 @@
 """Sharding the batched cells over ranks (CPU, gloo, world size 2).
 
 The cells of a batch are independent, so a multi-GPU run gives each rank a share and needs no
-collective on the data path.  Every rank computes the same largest-first assignment locally; the
-test checks, across two gloo ranks, that the shares cover every cell exactly once and balance the
-device bytes, and that the results gathered on the host come back in cell order."""
+collective on the data path.  Every rank computes the same largest-first assignment locally.
+Checked across two gloo ranks: the shares cover every cell exactly once and balance the device
+bytes; each rank solves its own cells (the oracle's periodic-cell solve, one host thread) and the
+results gathered on rank 0, put back in cell order, equal a single-process solve of all cells
+bit for bit (iterations, fluctuation field, mean stress)."""
 import os
 import socket
 
@@ -35,43 +37,74 @@ def test_partition_is_balanced_and_complete():
         assert max(loads) - min(loads) <= max(sizes)
 
 
-def _rank(rank, world, port, sizes, out_q):
+CELL_OPTS = dict(max_fmg_iter=0, nu1=2, nu2=2, sweeps=2, bottom=1, bottom_max_iter=200, bottom_reltol=1e-4, nuf=8,
+                 max_iter=100)
+
+
+def _work(ncells=10, seed=5):
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(ncells):
+        n = int(rng.choice([8, 12, 16]))
+        seeds, table = cells.rve_grains(n, int(rng.integers(3, 7)), int(rng.integers(1 << 30)))
+        out.append((n, seeds, table))
+    return out
+
+
+def _solve(work, idx):
+    """The oracle's cell solve of the cells idx (exx = 1e-3): {cell: (iters, w, mean stress)}."""
+    from anisotropicfracture_gb300 import models
+    from oracle import pyoracle as po
+    po.set_threads(1)
+    E = np.zeros((3, 3))
+    E[0, 0] = 1e-3
+    res = {}
+    for c in idx:
+        n, seeds, table = work[c]
+        L = po.rve_level(n)
+        Cf = cells.rve_stiffness(n, seeds, table)
+        w, st, rc, _ = po.rve_solve(L, models.MAJORMINOR, Cf, E, **CELL_OPTS)
+        assert rc == 0
+        res[c] = (int(st.iters), w, po.rve_mean_stress(L, models.MAJORMINOR, Cf, E, w))
+    return res
+
+
+def _rank(rank, world, port, out_q):
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
+    work = _work()
+    sizes = [n ** 3 for n, _, _ in work]
     mine = cells.partition_cells(sizes, world)[rank]
-    # each rank "solves" its cells (a stand-in value per cell) and the host gathers them
-    vals = torch.tensor([[c, 1000.0 + c] for c in mine], dtype=torch.float64)
-    n = torch.tensor([len(mine)])
-    ns = [torch.zeros(1, dtype=torch.long) for _ in range(world)]
-    dist.all_gather(ns, n)
-    width = int(max(x.item() for x in ns))
-    pad = torch.full((width, 2), -1.0, dtype=torch.float64)
-    pad[:len(mine)] = vals
-    got = [torch.zeros_like(pad) for _ in range(world)]
-    dist.all_gather(got, pad)
+    res = _solve(work, mine)  # this rank's share, no exchange on the data path
+    got = [None] * world
+    dist.all_gather_object(got, res)  # host-side gather of the results
     if rank == 0:
-        rows = torch.cat(got)
-        rows = rows[rows[:, 0] >= 0]
-        order = torch.argsort(rows[:, 0])
-        out_q.put(rows[order].numpy().tolist())
+        merged = {}
+        for part in got:
+            assert not set(part) & set(merged)
+            merged.update(part)
+        out_q.put([(c,) + merged[c] for c in sorted(merged)])
     dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_cover_every_cell_once():
+def test_two_gloo_ranks_solve_their_shares_like_one_process():
     import torch.multiprocessing as mp
-    rng = np.random.default_rng(5)
-    sizes = [int(e) ** 3 for e in rng.choice([16, 24, 32, 48, 64], size=37)]
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, sizes, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    rows = q.get(timeout=120)
+    rows = q.get(timeout=300)
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
-    assert [int(r[0]) for r in rows] == list(range(37))
-    assert all(r[1] == 1000.0 + r[0] for r in rows)
+    work = _work()
+    ref = _solve(work, range(len(work)))
+    assert [r[0] for r in rows] == list(range(len(work)))
+    for c, iters, w, sig in rows:
+        assert iters == ref[c][0]
+        assert np.array_equal(w, ref[c][1])
+        assert np.array_equal(sig, ref[c][2])
