@@ -106,6 +106,8 @@ SIGNATURES = {
     "ae_energy": ([P, C.c_int, FAB, FAB], C.c_int),
     "ae_newton_residual": ([P, C.c_int, FAB, FAB, FAB, FAB], C.c_int),
     "ae_newton_dw": ([P, C.c_int, FAB, FAB, FAB, FAB], C.c_int),
+    "ae_newton_neohookean": ([P, C.c_int, FAB, FAB, C.c_double, C.c_double, FAB], C.c_int),
+    "ae_neohookean_dw": ([P, C.c_int, FAB, C.c_double, C.c_double, FAB, FAB], C.c_int),
     "ae_solve": ([P, FAB, FAB, C.c_double, C.c_double, C.POINTER(SolverOpts), C.POINTER(SolveStats)], C.c_int),
     "ae_solveaffine": ([P, FAB, FAB, C.c_double, C.c_double, C.c_int, C.POINTER(SolverOpts), C.POINTER(SolveStats)],
                        C.c_int),

@@ -210,7 +210,9 @@ struct ae_op_s {
 
 namespace {
 
-int ncoef_of(int model) { return model == AE_MODEL_ISOTROPIC ? 2 : model == AE_MODEL_MAJORMINOR ? 21 : 9; }
+int ncoef_of(int model) {
+    return model == AE_MODEL_ISOTROPIC ? 2 : model == AE_MODEL_MAJORMINOR ? 21 : model == AE_MODEL_MAJOR ? 45 : 9;
+}
 
 // Orders the operator's own stream after earlier work on the legacy default stream and the
 // legacy stream after the work an entry point enqueued, so that callers that produce and
@@ -893,6 +895,38 @@ void solve_ml(ae_op* op, const ae_solver_opts& o, double tol_rel, double tol_abs
     if (!conv && o.fixed_iter <= 0) throw ApiErr(AE_ERR_NOT_CONVERGED, "MLMG failed to converge within max_iter");
 }
 
+// Host fabs handed to an entry point are staged through temporary device copies; out() copies
+// a result back, finish() waits for the copies when there were any, the destructor frees them.
+struct HostStage {
+    cudaStream_t st;
+    std::vector<void*> tmp;
+    explicit HostStage(cudaStream_t s) : st(s) {}
+    HostStage(const HostStage&) = delete;
+    HostStage& operator=(const HostStage&) = delete;
+    ~HostStage() {
+        for (void* p : tmp) cudaFree(p);
+    }
+    ae_fab in(const ae_fab& f) {
+        ae_fab d = f;
+        if (is_device_ptr(f.data)) return d;
+        const size_t bytes = sizeof(double) * (size_t)fab_elems(f);
+        void* p = nullptr;
+        AE_CHECK(cudaMalloc(&p, bytes));
+        tmp.push_back(p);
+        AE_CHECK(cudaMemcpyAsync(p, f.data, bytes, cudaMemcpyHostToDevice, st));
+        d.data = p;
+        return d;
+    }
+    void out(const ae_fab& host, const ae_fab& dev) {
+        if (dev.data != host.data)
+            AE_CHECK(cudaMemcpyAsync(host.data, dev.data, sizeof(double) * (size_t)fab_elems(host),
+                                     cudaMemcpyDeviceToHost, st));
+    }
+    void finish() {
+        if (!tmp.empty()) AE_CHECK(cudaStreamSynchronize(st));
+    }
+};
+
 }  // namespace
 
 // ===================================================================== C ABI
@@ -927,7 +961,7 @@ int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) 
         require(out != nullptr, "out is null");
         *out = nullptr;
         require(levels != nullptr && nlev >= 1, "need at least one level");
-        require(model >= 0 && model <= 2, "unknown model kind");
+        require(model >= 0 && model <= 3, "unknown model kind");
         std::unique_ptr<ae_op> op(new ae_op());
         op->model = model;
         op->ncoef = ncoef_of(model);
@@ -979,6 +1013,7 @@ int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) 
         if (const char* e = std::getenv("AE_TILED32")) op->tiled32 = std::atoi(e) != 0;
         if (const char* e = std::getenv("AE_TILED64")) op->tiled64 = std::atoi(e) != 0;
         if (const char* e = std::getenv("AE_SPLIT")) op->split32 = std::atoi(e) != 0;
+        if (model == AE_MODEL_MAJOR) op->tiled32 = op->tiled64 = false;  // per-node kernels only
         tiled_init<float>();
         tiled_init<double>();
         AE_CHECK(cudaMallocHost(&op->hnorm, 8 * sizeof(unsigned long long)));
@@ -1057,6 +1092,7 @@ int ae_op_set_model_grains(ae_op* op, int amrlev, const ae_fab* grain_id, int ng
     return guarded([&] {
         require(op != nullptr && table != nullptr, "null argument");
         require(ngrains >= 1 && ngrains <= 65535, "SetModelGrains: 1 to 65535 grains");
+        require(op->model != AE_MODEL_MAJOR, "SetModelGrains: not for the Sym::Major kind");
         StreamScope scope_(op);
         MGLevel& L = level_at(op, amrlev, 0);
         const Box3 need = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
@@ -1430,6 +1466,7 @@ int ae_stress(ae_op* op, int amrlev, const ae_fab* sig, const ae_fab* u, int voi
         const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
         check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "Stress u");
         check_fab(sig, v, voigt ? 6 : 9, "Stress sigma");
+        require(op->model != AE_MODEL_MAJOR, "Stress: the Sym::Major kind is a tangent (use NeoHookeanDW)");
         require(is_device_ptr(u->data) && is_device_ptr(sig->data), "Stress: fabs must be device memory");
         launch_stress(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
                       fab_view<double>(*sig), voigt, op->st);
@@ -1440,6 +1477,7 @@ int ae_newton_residual(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, 
     return guarded([&] {
         require(op != nullptr, "null operator");
         require(op->bc_set, "SetBC has not been called", AE_ERR_STATE);
+        require(op->model != AE_MODEL_MAJOR, "NewtonResidual: linear models only (use NewtonNeoHookean)");
         StreamScope scope_(op);
         MGLevel& L = level_at(op, amrlev, 0);
         require(op->amr[amrlev].model_set, "SetModel has not been called on this level", AE_ERR_STATE);
@@ -1456,32 +1494,63 @@ int ae_newton_residual(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, 
             op->newton_dw_n = 9 * L.nn;
         }
         // host fabs are staged through temporary device copies (rhs is copied back)
-        std::vector<void*> tmp;
-        auto on_device = [&](const ae_fab* f, bool copy_in) -> ae_fab {
-            ae_fab d = *f;
-            if (is_device_ptr(f->data)) return d;
-            const size_t bytes = sizeof(double) * (size_t)fab_elems(*f);
-            void* p = nullptr;
-            AE_CHECK(cudaMalloc(&p, bytes));
-            tmp.push_back(p);
-            if (copy_in) AE_CHECK(cudaMemcpyAsync(p, f->data, bytes, cudaMemcpyHostToDevice, op->st));
-            d.data = p;
-            return d;
-        };
-        struct Free {
-            std::vector<void*>& v;
-            ~Free() { for (void* p : v) cudaFree(p); }
-        } free_{tmp};
-        const ae_fab ud = on_device(u, true), bd = on_device(b, true), rd = on_device(rhs, true);
+        HostStage hs(op->st);
+        const ae_fab ud = hs.in(*u), bd = hs.in(*b), rd = hs.in(*rhs);
         ae_fab fd{};
-        if (F0) fd = on_device(F0, true);
+        if (F0) fd = hs.in(*F0);
         launch_newton_residual(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(ud)),
                                cview(fab_view<double>(bd)), F0 ? cview(fab_view<double>(fd)) : View<const double>{},
                                level_view(L.g, op->newton_dw), fab_view<double>(rd), op->st);
-        if (rd.data != rhs->data)
-            AE_CHECK(cudaMemcpyAsync(rhs->data, rd.data, sizeof(double) * (size_t)fab_elems(*rhs),
-                                     cudaMemcpyDeviceToHost, op->st));
-        if (!tmp.empty()) AE_CHECK(cudaStreamSynchronize(op->st));
+        hs.out(*rhs, rd);
+        hs.finish();
+    });
+}
+
+int ae_newton_neohookean(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, double mu, double kappa,
+                         ae_fab* rhs) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(op->bc_set, "SetBC has not been called", AE_ERR_STATE);
+        require(op->model == AE_MODEL_MAJOR, "NewtonNeoHookean: needs an operator of the Sym::Major kind");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 bx2 = box_isect(box_isect(box_grow(geo_valid(L.g), 2), geo_domain(L.g)), geo_store(L.g));
+        const Box3 bx1 = box_isect(box_isect(box_grow(geo_valid(L.g), 1), geo_domain(L.g)), geo_store(L.g));
+        check_fab(u, bx2, 3, "NewtonNeoHookean u");
+        check_fab(b, bx1, 3, "NewtonNeoHookean b");
+        check_fab(rhs, bx1, 3, "NewtonNeoHookean rhs");
+        require(!u->is_float && !b->is_float && !rhs->is_float, "NewtonNeoHookean: FP64 fields required");
+        if (op->newton_dw_n < 9 * L.nn) {
+            op->newton_dw = op->alloc<double>(9 * L.nn);
+            op->newton_dw_n = 9 * L.nn;
+        }
+        HostStage hs(op->st);
+        const ae_fab ud = hs.in(*u), bd = hs.in(*b), rd = hs.in(*rhs);
+        launch_neohookean_residual(op->params(L.g), cview(fab_view<double>(ud)), cview(fab_view<double>(bd)), mu,
+                                   kappa, level_view(L.g, L.C), level_view(L.g, op->newton_dw), fab_view<double>(rd),
+                                   op->st);
+        hs.out(*rhs, rd);
+        hs.finish();
+        L.grains = false;
+        op->amr[amrlev].model_set = true;
+        op->prepared = false;
+    });
+}
+
+int ae_neohookean_dw(ae_op* op, int amrlev, const ae_fab* u, double mu, double kappa, ae_fab* dw, ae_fab* w) {
+    return guarded([&] {
+        require(op != nullptr, "null operator");
+        require(dw || w, "NeoHookeanDW: nothing to compute");
+        StreamScope scope_(op);
+        MGLevel& L = level_at(op, amrlev, 0);
+        const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
+        check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "NeoHookeanDW u");
+        if (dw) check_fab(dw, v, 9, "NeoHookeanDW dw");
+        if (w) check_fab(w, v, 1, "NeoHookeanDW w");
+        require(is_device_ptr(u->data) && (!dw || is_device_ptr(dw->data)) && (!w || is_device_ptr(w->data)),
+                "NeoHookeanDW: fabs must be device memory");
+        launch_neohookean_post(L.g, cview(fab_view<double>(*u)), mu, kappa, dw ? fab_view<double>(*dw) : View<double>{},
+                               w ? fab_view<double>(*w) : View<double>{}, op->st);
     });
 }
 
@@ -1489,6 +1558,7 @@ int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fa
     return guarded([&] {
         require(op != nullptr, "null operator");
         require(dw || w, "NewtonDW: nothing to compute");
+        require(op->model != AE_MODEL_MAJOR, "NewtonDW: linear models only (use NeoHookeanDW)");
         StreamScope scope_(op);
         MGLevel& L = level_at(op, amrlev, 0);
         require(op->amr[amrlev].model_set, "SetModel has not been called on this level", AE_ERR_STATE);
@@ -1517,6 +1587,7 @@ int ae_energy(ae_op* op, int amrlev, const ae_fab* w, const ae_fab* u) {
         const Box3 v = box_isect(geo_valid(L.g), geo_domain(L.g));
         check_fab(u, box_isect(box_grow(v, 1), geo_domain(L.g)), 3, "Energy u");
         check_fab(w, v, 1, "Energy w");
+        require(op->model != AE_MODEL_MAJOR, "Energy: linear models only (use NeoHookeanDW)");
         require(is_device_ptr(u->data) && is_device_ptr(w->data), "Energy: fabs must be device memory");
         launch_energy(op->params(L.g), cview(level_view(L.g, L.C)), cview(fab_view<double>(*u)),
                       fab_view<double>(*w), op->st);

@@ -8,6 +8,7 @@
 //   MajorMinor C:grad src/Set/Matrix4_MajorMinor.H:253-269, C:gradgrad :287-345
 //   Isotropic         src/Set/Matrix4_Isotropic.H:60-91
 //   Diagonal          src/Set/Matrix4_Diagonal.H:48-74
+//   Major (45 slots)  src/Set/Matrix4_Major.H:198-300, 399-428
 //   boundary rows     src/BC/Operator/Elastic.H:218-303
 //   Fapply            src/Operator/Elastic.cpp:174-258
 #pragma once
@@ -15,11 +16,18 @@
 
 namespace ae {
 
-enum Model { ISO = 0, MM = 1, DIAG = 2 };
+enum Model { ISO = 0, MM = 1, DIAG = 2, MAJOR = 3 };
 template <int M> struct NCoef;
 template <> struct NCoef<ISO> { static constexpr int value = 2; };
 template <> struct NCoef<MM> { static constexpr int value = 21; };
 template <> struct NCoef<DIAG> { static constexpr int value = 9; };
+template <> struct NCoef<MAJOR> { static constexpr int value = 45; };
+
+// Set::Matrix4<3, Sym::Major>: the 9 x 9 matrix A(3i+j, 3k+l) = C_ijkl is symmetric; its upper
+// triangle is stored row by row in 45 slots.  Slot of entry (I, K).
+__host__ __device__ constexpr int major_slot(int I, int K) {
+    return I <= K ? I * 9 - I * (I - 1) / 2 + (K - I) : K * 9 - K * (K - 1) / 2 + (I - K);
+}
 
 enum BCType { DISP = 0, TRAC = 1, PERIODIC = 2, NEUMANN = 3 };
 
@@ -123,10 +131,26 @@ __device__ __forceinline__ void stress_diag(const R* a, const R g[3][3], R s[3][
 #pragma unroll
         for (int j = 0; j < 3; ++j) s[i][j] = a[3 * i + j] * g[i][j];
 }
+// Matrix4_Major.H:399-413: sigma_ij = sum_kl C_ijkl g_kl, summed in (k, l) order
+template <class R>
+__device__ __forceinline__ void stress_major(const R* a, const R g[3][3], R s[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            R r = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int l = 0; l < 3; ++l) r += a[major_slot(3 * i + j, 3 * k + l)] * g[k][l];
+            s[i][j] = r;
+        }
+}
 template <int M, class R>
 __device__ __forceinline__ void stress_of(const R* a, const R g[3][3], R s[3][3]) {
     if (M == ISO) stress_iso(a, g, s);
     else if (M == MM) stress_mm(a, g, s);
+    else if (M == MAJOR) stress_major(a, g, s);
     else stress_diag(a, g, s);
 }
 
@@ -175,10 +199,26 @@ __device__ __forceinline__ void div_diag(const R* a, const R b[3][3][3], R f[3])
         f[i] = r;
     }
 }
+// Matrix4_Major.H:415-428: f_i = sum_{j,k,l} C_ijkl b[k][l][j], b[k][l][j] = u_{k,lj}
+template <class R>
+__device__ __forceinline__ void div_major(const R* a, const R b[3][3][3], R f[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        R r = R(0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int l = 0; l < 3; ++l) r += a[major_slot(3 * i + j, 3 * k + l)] * b[k][l][j];
+        f[i] = r;
+    }
+}
 template <int M, class R>
 __device__ __forceinline__ void div_of(const R* a, const R b[3][3][3], R f[3]) {
     if (M == ISO) div_iso(a, b, f);
     else if (M == MM) div_mm(a, b, f);
+    else if (M == MAJOR) div_major(a, b, f);
     else div_diag(a, b, f);
 }
 
@@ -225,6 +265,16 @@ __device__ __forceinline__ void gradC_col(const R* __restrict__ C, long long cs,
             col[0] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
             col[1] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
             col[2] = a5 * e00 + a10 * e01 + a14 * e02 + a17 * e11 + a19 * e12 + a20 * e22;
+        }
+    } else if (M == MAJOR) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            R v = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int l = 0; l < 3; ++l) v += DC(major_slot(3 * r + d, 3 * k + l)) * g[k][l];
+            col[r] = v;
         }
     } else if (M == ISO) {
         const R dl = DC(0), dm = DC(1);
@@ -275,6 +325,16 @@ __device__ __forceinline__ void gradC_col_f(F&& dC, const R g[3][3], int d, R co
             col[1] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
             col[2] = a5 * e00 + a10 * e01 + a14 * e02 + a17 * e11 + a19 * e12 + a20 * e22;
         }
+    } else if (M == MAJOR) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            R v = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int l = 0; l < 3; ++l) v += dC(major_slot(3 * r + d, 3 * k + l)) * g[k][l];
+            col[r] = v;
+        }
     } else if (M == ISO) {
         const R dl = dC(0), dm = dC(1);
         const R tr = dl * (g[0][0] + g[1][1] + g[2][2]);
@@ -314,6 +374,7 @@ template <> struct ZSlots<DIAG> {
     static constexpr int n = 3;
     __device__ static constexpr int at(int s) { return 3 * s + 2; }
 };
+
 // position of slot q in the ZSlots list (-1 if absent)
 template <int M>
 __device__ __forceinline__ constexpr int zslot_index(int q) {

@@ -682,5 +682,12 @@ inline void dispatch_model(int model, F&& f) {
     else if (model == MM) f(std::integral_constant<int, MM>());
     else f(std::integral_constant<int, DIAG>());
 }
+// the box operator's kinds: the three above and the 45-slot Sym::Major tangent of a
+// finite-kinematics model
+template <class R, class F>
+inline void dispatch_model4(int model, F&& f) {
+    if (model == MAJOR) f(std::integral_constant<int, MAJOR>());
+    else dispatch_model<R>(model, f);
+}
 
 }  // namespace ae

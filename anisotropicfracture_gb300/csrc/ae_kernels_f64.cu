@@ -414,6 +414,127 @@ void launch_newton_post(const OpParams& P, View<const double> C, View<const doub
     launched();
 }
 
+// ------------------------------------------------------------------ NeoHookean (finite kinematics)
+// Model::Solid::Elastic::NeoHookean (src/Model/Solid/Elastic/NeoHookean.H:19-66) at F = I + grad u.
+// G = F^-T is the signed cofactor matrix of F times 1 / det F; J23 = |det F|^(2/3); tr = F : F.
+struct NeoKin {
+    double F[3][3], G[3][3], J, J23, tr;
+};
+__device__ __forceinline__ void neo_kin(const double gu[3][3], NeoKin& n) {
+    for (int p = 0; p < 3; ++p)
+        for (int d = 0; d < 3; ++d) n.F[p][d] = gu[p][d] + (p == d ? 1.0 : 0.0);
+    const auto& F = n.F;
+    double cof[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+            cof[i][j] = F[i1][j1] * F[i2][j2] - F[i1][j2] * F[i2][j1];
+        }
+    n.J = F[0][0] * cof[0][0] + F[1][0] * cof[1][0] + F[2][0] * cof[2][0];
+    const double inv = 1.0 / n.J;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) n.G[i][j] = cof[i][j] * inv;
+    n.J23 = pow(fabs(n.J), 2. / 3.);
+    double tr = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) tr += F[i][j] * F[i][j];
+    n.tr = tr;
+}
+// NeoHookean::DW (NeoHookean.H:28-39): mu (F / J23 - tr G / (3 J23)) + kappa (J - 1) J G
+__device__ __forceinline__ void neo_dw(const NeoKin& n, double mu, double kappa, double dw[3][3]) {
+    const double a = kappa * (n.J - 1) * n.J;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            dw[i][j] = mu * (n.F[i][j] / n.J23 - n.tr * n.G[i][j] / (3. * n.J23)) + a * n.G[i][j];
+}
+// NeoHookean::DDW (NeoHookean.H:40-66) entry (i, j, k, l)
+__device__ __forceinline__ double neo_ddw(const NeoKin& n, double mu, double kappa, int i, int j, int k, int l) {
+    const auto& F = n.F;
+    const auto& G = n.G;
+    double t1 = 0.0, t2 = 0.0;
+    if (i == k && j == l) t1 += 1.0;
+    t1 -= (2. / 3.) * F[i][j] * G[k][l];
+    t1 -= (2. / 3.) * G[i][j] * F[k][l];
+    t1 += (2. / 9.) * n.tr * G[i][j] * G[k][l];
+    t1 += (1. / 3.) * n.tr * G[i][l] * G[k][j];
+    t2 += (2. * n.J - 1.) * G[i][j] * G[k][l];
+    t2 += (1. - n.J) * G[i][l] * G[k][j];
+    return (mu / n.J23) * t1 + kappa * n.J * t2;
+}
+// Newton::prepareForSolve with kinematic variable F (src/Solver/Nonlocal/Newton.H:45-76) on
+// bx2 = grow(valid, 2) ∩ domain: dw = DW(F), and the level's stiffness C = DDW(F) in the 45
+// Sym::Major slots.  The reference assigns ddw(i,j,k,l) in (i, j, k, l) order through the shared
+// slot of A(3i+j, 3k+l) and A(3k+l, 3i+j), so each slot ends up holding the value evaluated with
+// (i, j) the larger row index of the pair: that is the evaluation made here.
+__global__ void __launch_bounds__(kBlock) k_neohookean(SCoef<double> K, Reg reg, Box3 bx2, View<const double> u,
+                                                       double mu, double kappa, View<double> dw, View<double> C) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3], w[3][3];
+    grad_box(bx2, K, u, i, j, k, gu);
+    NeoKin n;
+    neo_kin(gu, n);
+    neo_dw(n, mu, kappa, w);
+    const long long o = dw.at(i, j, k);
+    for (int p = 0; p < 3; ++p)
+        for (int d = 0; d < 3; ++d) dw.p[o + (3 * p + d) * dw.sc] = w[p][d];
+    const long long oc = C.at(i, j, k);
+#pragma unroll
+    for (int I = 0; I < 9; ++I)
+#pragma unroll
+        for (int Kk = I; Kk < 9; ++Kk)
+            C.p[oc + major_slot(I, Kk) * C.sc] = neo_ddw(n, mu, kappa, Kk / 3, Kk % 3, I / 3, I % 3);
+}
+// Newton::W and Newton::DW with kinematic variable F on valid ∩ domain, stencils relative to
+// the domain (src/Solver/Nonlocal/Newton.H:233-333)
+__global__ void __launch_bounds__(kBlock) k_neohookean_post(Geo g, SCoef<double> K, Reg reg, View<const double> u,
+                                                            double mu, double kappa, View<double> dw,
+                                                            View<double> w) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    double gu[3][3];
+    grad_at(g, K, u, i, j, k, gu);
+    NeoKin n;
+    neo_kin(gu, n);
+    if (dw.p) {
+        double s[3][3];
+        neo_dw(n, mu, kappa, s);
+        const long long o = dw.at(i, j, k);
+        for (int p = 0; p < 3; ++p)
+            for (int d = 0; d < 3; ++d) dw.p[o + (3 * p + d) * dw.sc] = s[p][d];
+    }
+    // NeoHookean::W (NeoHookean.H:19-27)
+    if (w.p) {
+        double e = 0.0;
+        e += 0.5 * mu * (n.tr / n.J23 - 3.);
+        e += 0.5 * kappa * (n.J - 1.0) * (n.J - 1.0);
+        w.p[w.at(i, j, k)] = e;
+    }
+}
+void launch_neohookean_residual(const OpParams& P, View<const double> u, View<const double> b, double mu,
+                                double kappa, View<double> C, View<double> dw, View<double> rhs, cudaStream_t st) {
+    const Box3 bx2 = box_isect(box_isect(box_grow(geo_valid(P.g), 2), geo_domain(P.g)), geo_store(P.g));
+    const Box3 bx1 = box_isect(box_isect(box_grow(geo_valid(P.g), 1), geo_domain(P.g)), geo_store(P.g));
+    const SCoef<double> K = make_scoef<double>(P.g);
+    const Reg r2 = make_reg(bx2), r1 = make_reg(bx1);
+    if (r2.n == 0) return;
+    k_neohookean<<<nblocks(r2.n), kBlock, 0, st>>>(K, r2, bx2, u, mu, kappa, dw, C);
+    launched();
+    k_newton_rhs<<<nblocks(r1.n), kBlock, 0, st>>>(P.g, P.bc, K, r1, bx1, u, b, cview(dw), rhs);
+    launched();
+}
+void launch_neohookean_post(const Geo& g, View<const double> u, double mu, double kappa, View<double> dw,
+                            View<double> w, cudaStream_t st) {
+    const Reg reg = make_reg(box_isect(geo_valid(g), geo_domain(g)));
+    if (reg.n == 0) return;
+    k_neohookean_post<<<nblocks(reg.n), kBlock, 0, st>>>(g, make_scoef<double>(g), reg, u, mu, kappa, dw, w);
+    launched();
+}
+
 // ------------------------------------------------------------------ bottom solve (one CTA)
 // MLMG::actualBottomSolve + MLCGSolver::solve_cg / solve_bicgstab (krylov_bottom); the whole
 // Krylov loop runs inside one thread block on the coarsest level (ng = 0, storage = domain).
@@ -532,7 +653,7 @@ __host__ __device__ constexpr long long bottom_smem_doubles(int nc, long long nn
 // Levels whose arrays fit the default 48 KB of dynamic shared memory (no function attribute,
 // so the launch is legal inside stream capture) run from shared memory; larger ones from global.
 void launch_bottom(const BottomArgs& a, cudaStream_t st) {
-    dispatch_model<double>(a.P.model, [&](auto m) {
+    dispatch_model4<double>(a.P.model, [&](auto m) {
         constexpr int Mv = decltype(m)::value;
         const size_t bytes = (size_t)bottom_smem_doubles(NCoef<Mv>::value, a.nn) * sizeof(double);
         if (bytes <= kBottomSmemBytes) k_bottom<Mv, true><<<1, kBottomThreads, bytes, st>>>(a);
@@ -604,7 +725,7 @@ __global__ void __launch_bounds__(128) k_bottom_assemble(BottomArgs a, double* A
     }
 }
 void launch_bottom_assemble(const BottomArgs& a, double* A, double* E, cudaStream_t st) {
-    dispatch_model<double>(a.P.model, [&](auto m) {
+    dispatch_model4<double>(a.P.model, [&](auto m) {
         k_bottom_assemble<decltype(m)::value><<<(unsigned)(3 * a.nn), 128, 0, st>>>(a, A, E);
     });
     launched();

@@ -167,6 +167,13 @@ void launch_newton_residual(const OpParams& P, View<const double> C, View<const 
 // Newton::DW (dw.p may be null) and Newton::W (w.p may be null) on valid ∩ domain
 void launch_newton_post(const OpParams& P, View<const double> C, View<const double> u, View<const double> F0,
                         View<double> dw, View<double> w, double half, cudaStream_t st);
+// Newton<NeoHookean>: dw = DW(I + grad u) and C = DDW(I + grad u) (45 Sym::Major slots) on
+// grow(valid, 2) ∩ domain, then rhs = b - N(u) on grow(valid, 1) ∩ domain
+void launch_neohookean_residual(const OpParams& P, View<const double> u, View<const double> b, double mu,
+                                double kappa, View<double> C, View<double> dw, View<double> rhs, cudaStream_t st);
+// NeoHookean DW (dw.p may be null) and W (w.p may be null) on valid ∩ domain
+void launch_neohookean_post(const Geo& g, View<const double> u, double mu, double kappa, View<double> dw,
+                            View<double> w, cudaStream_t st);
 // Voronoi stiffness over `region`: ids (int32 per node) -> gid (uint16) and the per-node FP64
 // stiffness C = tab[id]; tab32 = (float) tab.  *bad is set if an id is outside [0, ng).
 void launch_grains_box(const Box3& region, View<const int> ids, View<unsigned short> gid, View<double> C,

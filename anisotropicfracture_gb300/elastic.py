@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import AeError, Fab, LevelDesc, SolveStats, check, default_opts, load
-from .models import DIAGONAL, ISOTROPIC, MAJORMINOR, NCOEF
+from .models import DIAGONAL, ISOTROPIC, MAJOR, MAJORMINOR, NCOEF, NeoHookean
 
 FACES = ["XLO", "YLO", "ZLO", "XHI", "YHI", "ZHI",
          "YLO_ZLO", "YLO_ZHI", "YHI_ZLO", "YHI_ZHI",
@@ -286,6 +286,23 @@ class Elastic:
         check(load().ae_newton_dw(self._h, amrlev, C.byref(fu), C.byref(f0) if f0 is not None else None,
                                   C.byref(fd) if fd is not None else None, C.byref(fw) if fw is not None else None))
 
+    def NewtonNeoHookean(self, amrlev, rhs, u, b, model):
+        """Newton<NeoHookean>::prepareForSolve on one level: the level's stiffness becomes
+        DDW(I + grad u) and rhs = b - N(u) with DW(I + grad u) (ae_newton_neohookean).  The
+        operator is of kind models.MAJOR; host or device Fields."""
+        fr, fu, fb = rhs.fab(), u.fab(), b.fab()
+        check(load().ae_newton_neohookean(self._h, amrlev, C.byref(fu), C.byref(fb), float(model.mu),
+                                          float(model.kappa), C.byref(fr)))
+
+    def NeoHookeanDW(self, amrlev, u, model, dw=None, w=None):
+        """Newton<NeoHookean>::DW (9 components) and ::W at F = I + grad u; device Fields."""
+        fu = u.fab()
+        fd = dw.fab() if dw is not None else None
+        fw = w.fab() if w is not None else None
+        check(load().ae_neohookean_dw(self._h, amrlev, C.byref(fu), float(model.mu), float(model.kappa),
+                                      C.byref(fd) if fd is not None else None,
+                                      C.byref(fw) if fw is not None else None))
+
     def Energy(self, amrlev, energy, u, homogeneous=False):
         fw, fu = energy.fab(), u.fab()
         check(load().ae_energy(self._h, amrlev, C.byref(fw), C.byref(fu)))
@@ -387,10 +404,14 @@ class Linear:
 
 
 class Newton(Linear):
-    """Solver::Nonlocal::Newton<T> (src/Solver/Nonlocal/Newton.H:141-205) for the linear and
-    affine models: m_nriters times, rhs = b - N(u) (ae_newton_residual), one Linear::solve of the
-    correction (its previous value is the initial guess, as the reference keeps dsol), u += dsol.
-    F0: per-level eigenstrain Fields (9 components) of an Affine model, or None."""
+    """Solver::Nonlocal::Newton<T> (src/Solver/Nonlocal/Newton.H:141-205): m_nriters times,
+    rhs = b - N(u), one Linear::solve of the correction (its previous value is the initial guess,
+    as the reference keeps dsol), u += dsol.  For the linear and affine models the operator's
+    stiffness is fixed and N(u) = div(C : (grad u - F0)) (ae_newton_residual; F0: per-level
+    eigenstrain Fields, 9 components, of an Affine model, or None).  With model a
+    models.NeoHookean the operator is of kind models.MAJOR and every iteration first sets its
+    stiffness to the tangent DDW(I + grad u) and N(u) = div DW(I + grad u)
+    (ae_newton_neohookean)."""
 
     def __init__(self, op):
         super().__init__(op)
@@ -440,6 +461,9 @@ class Newton(Linear):
         res = None
         for _ in range(self.m_nriters):
             for lev in range(len(ud)):
+                if isinstance(model, NeoHookean):
+                    self.linop.NewtonNeoHookean(lev, rhs[lev], ud[lev], bd[lev], model)
+                    continue
                 fu, fb, fr = ud[lev].fab(), bd[lev].fab(), rhs[lev].fab()
                 f0 = fd[lev].fab() if fd[lev] is not None else None
                 check(load().ae_newton_residual(self.linop.handle, lev, C.byref(fu), C.byref(fb),

@@ -5,11 +5,39 @@ Model::Solid::Affine::Isotropic.  Coefficient layouts:
   ISOTROPIC  (lambda, mu)                     Set::Matrix4<3,Sym::Isotropic>  (src/Set/Matrix4_Isotropic.H:12-15)
   MAJORMINOR 21 slots                          Set::Matrix4<3,Sym::MajorMinor> (src/Set/Matrix4_MajorMinor.H:145-192)
   DIAGONAL   A(i,j) row-major                  Set::Matrix4<3,Sym::Diagonal>   (src/Set/Matrix4_Diagonal.H:117-126)
+  MAJOR      45 slots: upper triangle of the 9 x 9 matrix A(3i+j, 3k+l), row by row
+                                               Set::Matrix4<3,Sym::Major>      (src/Set/Matrix4_Major.H:203-258)
+and the finite-kinematics Model::Solid::Elastic::NeoHookean, whose tangent is a MAJOR field.
 """
+from dataclasses import dataclass
+
 import numpy as np
 
-ISOTROPIC, MAJORMINOR, DIAGONAL = 0, 1, 2
-NCOEF = {ISOTROPIC: 2, MAJORMINOR: 21, DIAGONAL: 9}
+ISOTROPIC, MAJORMINOR, DIAGONAL, MAJOR = 0, 1, 2, 3
+NCOEF = {ISOTROPIC: 2, MAJORMINOR: 21, DIAGONAL: 9, MAJOR: 45}
+
+
+@dataclass
+class NeoHookean:
+    """Model::Solid::Elastic::NeoHookean (src/Model/Solid/Elastic/NeoHookean.H:11-81): W(F) =
+    mu/2 (F:F / |J|^(2/3) - 3) + kappa/2 (J - 1)^2 with kinematic variable F = I + grad u."""
+    mu: float
+    kappa: float
+
+
+def major_slot(I, K):
+    """Slot of entry (I, K) of the 9 x 9 matrix of a Sym::Major tensor."""
+    if I > K:
+        I, K = K, I
+    return I * 9 - I * (I - 1) // 2 + (K - I)
+
+
+def major_from_full(T):
+    """45 Sym::Major slots of tensors shaped (..., 3, 3, 3, 3) (upper triangle of A(3i+j, 3k+l));
+    returns (..., 45)."""
+    A = np.asarray(T, dtype=np.float64).reshape(np.shape(T)[:-4] + (9, 9))
+    rows, cols = np.triu_indices(9)
+    return A[..., rows, cols]
 
 # Voigt index of an index pair and the 21 storage slots of the reference's MajorMinor
 # tensor, keyed by the (sorted) pair of Voigt indices: the table restates the uid map of

@@ -45,8 +45,18 @@ typedef enum {
 /* Per-node stiffness kinds (Model::Solid::Solid<Sym>::ddw storage).
  *  ISOTROPIC : 2 coefficients (lambda, mu)        Set::Matrix4<3,Sym::Isotropic>
  *  MAJORMINOR: 21 coefficients (reference slots)   Set::Matrix4<3,Sym::MajorMinor>
- *  DIAGONAL  : 9 coefficients A(i,j), row-major    Set::Matrix4<3,Sym::Diagonal>   */
-typedef enum { AE_MODEL_ISOTROPIC = 0, AE_MODEL_MAJORMINOR = 1, AE_MODEL_DIAGONAL = 2 } ae_model_kind;
+ *  DIAGONAL  : 9 coefficients A(i,j), row-major    Set::Matrix4<3,Sym::Diagonal>
+ *  MAJOR     : 45 coefficients, the upper triangle of the 9 x 9 matrix A(3i+j, 3k+l) row by row
+ *              (src/Set/Matrix4_Major.H:203-258)  Set::Matrix4<3,Sym::Major>: the tangent
+ *              DDW of a finite-kinematics model (Model::Solid::Elastic::NeoHookean).  No grain
+ *              maps (ae_op_set_model_grains), no Stress / Energy / NewtonResidual / NewtonDW
+ *              (those evaluate a linear model); ae_newton_neohookean sets it.            */
+typedef enum {
+    AE_MODEL_ISOTROPIC = 0,
+    AE_MODEL_MAJORMINOR = 1,
+    AE_MODEL_DIAGONAL = 2,
+    AE_MODEL_MAJOR = 3
+} ae_model_kind;
 
 /* BC::Operator::Elastic<T>::Type, same numbering (src/BC/Operator/Elastic.H:24) */
 typedef enum { AE_BC_DISPLACEMENT = 0, AE_BC_TRACTION = 1, AE_BC_PERIODIC = 2, AE_BC_NEUMANN = 3 } ae_bc_type;
@@ -211,6 +221,18 @@ int ae_newton_residual(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, 
  * G = grad u - F0, except Affine::Isotropic (isotropic model with F0) whose W has no 1/2
  * (src/Model/Solid/Affine/Isotropic.H:31-34). */
 int ae_newton_dw(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* F0, ae_fab* dw, ae_fab* w);
+/* Newton<Model::Solid::Elastic::NeoHookean>::prepareForSolve (src/Solver/Nonlocal/Newton.H:30-139
+ * with kinematic variable F; src/Model/Solid/Elastic/NeoHookean.H:28-66): at F = I + grad u,
+ * node by node over grow(valid, 2) ∩ domain, the level's stiffness becomes DDW(F) (what
+ * Elastic<Sym::Major>::SetModel then copies) and DW(F) feeds rhs = b - N(u) on
+ * grow(valid, 1) ∩ domain as in ae_newton_residual.  The operator must be of kind
+ * AE_MODEL_MAJOR; fab extents, types and memory as ae_newton_residual.  Marks the operator
+ * unprepared (ae_solve prepares it again). */
+int ae_newton_neohookean(ae_op* op, int amrlev, const ae_fab* u, const ae_fab* b, double mu, double kappa,
+                         ae_fab* rhs);
+/* Newton<NeoHookean>::DW (9 components, row-major) and ::W on valid ∩ domain with F = I + grad u,
+ * stencils as ae_newton_dw; device fabs, either output may be NULL. */
+int ae_neohookean_dw(ae_op* op, int amrlev, const ae_fab* u, double mu, double kappa, ae_fab* dw, ae_fab* w);
 
 /* Solver::Nonlocal::Linear::solve (Linear.H:102-112) -> MLMG::solve.
  * sol and rhs: one fab per AMR level, host or device; sol holds the initial guess.

@@ -176,6 +176,36 @@ struct Cubic {
     void coeffs(double* c) const { for (int q = 0; q < 21; ++q) c[q] = ddw[q]; }
 };
 }  // namespace Linear
+namespace Elastic {
+// Elastic::NeoHookean (src/Model/Solid/Elastic/NeoHookean.H:11-81), kinematic variable
+// F = I + grad u.  Its per-node tangent DDW(F) is a Sym::Major field (45 slots), which
+// Newton<NeoHookean> evaluates on the device (ae_newton_neohookean); coeffs() gives DDW(I),
+// the small-strain tangent, for a uniform SetModel.
+struct NeoHookean {
+    static constexpr int kind = AE_MODEL_MAJOR;
+    static constexpr int ncoef = 45;
+    double mu = 0, kappa = 0;
+    NeoHookean() = default;
+    NeoHookean(double a_mu, double a_kappa) : mu(a_mu), kappa(a_kappa) {}
+    // NeoHookean::DDW (NeoHookean.H:40-66) at F = I: G = F^-T = I, J = 1, F:F = 3
+    void coeffs(double* c) const {
+        const double d[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int I = 0; I < 9; ++I)
+            for (int K = I; K < 9; ++K) {
+                const int i = K / 3, j = K % 3, k = I / 3, l = I % 3;
+                double t1 = 0.0, t2 = 0.0;
+                if (i == k && j == l) t1 += 1.0;
+                t1 -= (2. / 3.) * d[i][j] * d[k][l];
+                t1 -= (2. / 3.) * d[i][j] * d[k][l];
+                t1 += (2. / 9.) * 3.0 * d[i][j] * d[k][l];
+                t1 += (1. / 3.) * 3.0 * d[i][l] * d[k][j];
+                t2 += (2. * 1.0 - 1.) * d[i][j] * d[k][l];
+                t2 += (1. - 1.0) * d[i][l] * d[k][j];
+                c[I * 9 - I * (I - 1) / 2 + (K - I)] = mu * t1 + kappa * t2;
+            }
+    }
+};
+}  // namespace Elastic
 }  // namespace Solid
 }  // namespace Model
 
@@ -238,7 +268,7 @@ public:
     }
     // SetModel(T&): one stiffness everywhere (Elastic.cpp:57-82)
     void SetModel(const T& model) {
-        double c[21];
+        double c[T::ncoef];
         model.coeffs(c);
         alamo::check(ae_op_set_model_uniform(m_op, c, T::ncoef));
     }
@@ -255,7 +285,7 @@ public:
                          const std::vector<double>* F0tab = nullptr, alamo::Fab* F0 = nullptr) {
         std::vector<double> tab(phases.size() * T::ncoef);
         for (size_t n = 0; n < phases.size(); ++n) {
-            double c[21];
+            double c[T::ncoef];
             phases[n].coeffs(c);
             for (int q = 0; q < T::ncoef; ++q) tab[n * T::ncoef + q] = c[q];
         }
@@ -353,10 +383,12 @@ protected:
     double m_tol_rel = 1e-8, m_tol_abs = 1e-8;
 };
 
-// Newton<T>::solve (src/Solver/Nonlocal/Newton.H:141-205) for the linear and affine models:
-// m_nriters times, rhs = b - N(u) (ae_newton_residual), one Linear::solve of the correction
-// (starting from the previous correction, as the reference keeps dsol), u += dsol.  F0: one
-// 9-component eigenstrain fab per level for an Affine model, or none.
+// Newton<T>::solve (src/Solver/Nonlocal/Newton.H:141-205): m_nriters times, rhs = b - N(u), one
+// Linear::solve of the correction (starting from the previous correction, as the reference
+// keeps dsol), u += dsol.  Linear and affine models: rhs from ae_newton_residual (F0: one
+// 9-component eigenstrain fab per level for an Affine model, or none).  NeoHookean: pass the
+// model; every iteration sets the operator's stiffness to DDW(I + grad u) and forms rhs with
+// DW(I + grad u) (ae_newton_neohookean).
 template <class T>
 class Newton : public Linear {
 public:
@@ -364,6 +396,16 @@ public:
     void setNRIters(int n) { m_nriters = n; }
     double solve(std::vector<alamo::Fab>& u, std::vector<alamo::Fab>& b, double tol_rel, double tol_abs,
                  const std::vector<alamo::Fab>* F0 = nullptr) {
+        return run(u, b, tol_rel, tol_abs, F0, nullptr);
+    }
+    double solve(std::vector<alamo::Fab>& u, std::vector<alamo::Fab>& b, const T& model, double tol_rel,
+                 double tol_abs) {
+        return run(u, b, tol_rel, tol_abs, nullptr, &model);
+    }
+
+private:
+    double run(std::vector<alamo::Fab>& u, std::vector<alamo::Fab>& b, double tol_rel, double tol_abs,
+               const std::vector<alamo::Fab>* F0, const T* model) {
         const size_t nl = u.size();
         std::vector<std::vector<double>> dbuf(nl), rbuf(nl);
         std::vector<alamo::Fab> dsol(nl), rhs(nl);
@@ -379,6 +421,11 @@ public:
             for (size_t l = 0; l < nl; ++l) {
                 const ae_fab fu = u[l].c(), fb = b[l].c();
                 ae_fab fr = rhs[l].c();
+                if (model && T::kind == AE_MODEL_MAJOR) {
+                    alamo::check(ae_newton_neohookean(m_op.handle(), (int)l, &fu, &fb, model_mu(*model),
+                                                      model_kappa(*model), &fr));
+                    continue;
+                }
                 ae_fab f0{};
                 if (F0) f0 = (*F0)[l].c();
                 alamo::check(ae_newton_residual(m_op.handle(), (int)l, &fu, &fb, F0 ? &f0 : nullptr, &fr));
@@ -389,8 +436,17 @@ public:
         }
         return res;
     }
+    template <class M>
+    static double model_mu(const M& m) {
+        if constexpr (M::kind == AE_MODEL_MAJOR) return m.mu;
+        else return 0.0;
+    }
+    template <class M>
+    static double model_kappa(const M& m) {
+        if constexpr (M::kind == AE_MODEL_MAJOR) return m.kappa;
+        else return 0.0;
+    }
 
-private:
     Operator::Elastic<T>& m_op;
     int m_nriters = 1;
 };

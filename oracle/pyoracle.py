@@ -399,13 +399,15 @@ def neohookean_ddw(F, mu, kappa):
 
 def major45(ddw):
     """Set::Matrix4<3, Sym::Major> storage (src/Set/Matrix4_Major.H:203-258) of tensors shaped
-    (..., 3, 3, 3, 3): the upper triangle of the 9 x 9 matrix A(3i+j, 3k+l), row by row; returned
-    as (45, ...) per-node coefficient fields.  Entries below the diagonal are taken from above
-    (the tensor is assumed major-symmetric)."""
+    (..., 3, 3, 3, 3): slot s of the upper triangle (I, K), I <= K, of the 9 x 9 matrix
+    A(3i+j, 3k+l), row by row; returned as (45, ...) per-node coefficient fields.  A slot holds
+    the entry (K, I) below the diagonal: NeoHookean::DDW (NeoHookean.H:44-63) assigns both
+    entries of a pair through the one slot in (i, j, k, l) order, so the lower one is written
+    last and kept (the tensor is major-symmetric up to rounding)."""
     ddw = np.asarray(ddw, dtype=np.float64)
     A = ddw.reshape(ddw.shape[:-4] + (9, 9))
     rows, cols = np.triu_indices(9)
-    return np.ascontiguousarray(np.moveaxis(A[..., rows, cols], -1, 0))
+    return np.ascontiguousarray(np.moveaxis(A[..., cols, rows], -1, 0))
 
 
 def neohookean_newton(L, mu, kappa, bctype, u, b, nriters=6, tol_rel=1e-10, tol_abs=0.0, **kw):

@@ -129,3 +129,13 @@ def cubic_define(C11, C12, C44, R):
 
 def level(*a, **k):
     return po.level(*a, **k)
+
+
+def neohookean(mu, kappa, F):
+    """Model::Solid::Elastic::NeoHookean W, DW and DDW of the reference at deformation gradients F
+    (n, 3, 3): returns (w (n,), dw (n, 3, 3), ddw (n, 45) in the Sym::Major slot order)."""
+    F = np.ascontiguousarray(np.asarray(F, dtype=np.float64).reshape(-1, 9))
+    n = F.shape[0]
+    w, dw, ddw = np.zeros(n), np.zeros((n, 9)), np.zeros((n, 45))
+    _check(lib().ref_neohookean(C.c_double(mu), C.c_double(kappa), n, _d(F), _d(w), _d(dw), _d(ddw)))
+    return w, dw.reshape(n, 3, 3), ddw

@@ -26,6 +26,7 @@
 #include "Model/Solid/Linear/Isotropic.H"
 #include "Model/Solid/Linear/Cubic.H"
 #include "Model/Solid/Linear/Laplacian.H"
+#include "Model/Solid/Elastic/NeoHookean.H"
 #include "BC/Operator/Elastic.H"
 
 using namespace amrex;
@@ -121,6 +122,7 @@ using Op = ::Operator::Elastic<T>;
 using Iso = Model::Solid::Linear::Isotropic;
 using Cub = Model::Solid::Linear::Cubic;
 using Lap = Model::Solid::Linear::Laplacian;
+using Neo = Model::Solid::Elastic::NeoHookean;
 
 // One model per node from the oracle's coefficient layout [slot][k][j][i].
 Iso make_model(const Iso*, const double* C, long n, long p, const int*) { return Iso(C[p + n], C[p]); }  // (mu, lambda)
@@ -140,6 +142,16 @@ Lap make_model(const Lap*, const double* C, long n, long p, const int*) {
     Model::Solid::Solid<Set::Sym::Diagonal> base;
     base.ddw = Set::Matrix4<3, Set::Sym::Diagonal>(A);
     return Lap(base);
+}
+
+// Elastic<NeoHookean> reads only the tangent ddw (a Sym::Major tensor): the 45 slots in
+// upper-triangle order, written through the tensor's (i, j, k, l) accessor
+Neo make_model(const Neo*, const double* C, long n, long p, const int*) {
+    Neo m;
+    int s = 0;
+    for (int I = 0; I < 9; I++)
+        for (int K = I; K < 9; K++, s++) m.ddw(I / 3, I % 3, K / 3, K % 3) = C[p + n * s];
+    return m;
 }
 
 template <class T>
@@ -190,6 +202,7 @@ int dispatch(int model, A... a) {
         case 0: return guarded([&] { Fn<Iso>::run(a...); });
         case 1: return guarded([&] { Fn<Cub>::run(a...); });
         case 2: return guarded([&] { Fn<Lap>::run(a...); });
+        case 3: return guarded([&] { Fn<Neo>::run(a...); });
     }
     g_err = "unknown model kind";
     return -2;
@@ -270,6 +283,11 @@ struct AvgDownFn {  // stiffness of the level below (coarsened by 2): averageDow
     static void read_coeffs(Lap& m, double* Cc, long n, long p, const int*) {
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) Cc[p + n * (3 * i + j)] = m.ddw(i, j, i, j);
+    }
+    static void read_coeffs(Neo& m, double* Cc, long n, long p, const int*) {
+        int s = 0;
+        for (int I = 0; I < 9; I++)
+            for (int K = I; K < 9; K++, s++) Cc[p + n * s] = m.ddw(I / 3, I % 3, K / 3, K % 3);
     }
 };
 template <class T>
@@ -354,6 +372,31 @@ int ref_cubic_define(double C11, double C12, double C44, const double* R, const 
             for (int j = 0; j < 3; j++)
                 for (int k = 0; k < 3; k++)
                     for (int l = 0; l < 3; l++) out21[slot81[((i * 3 + j) * 3 + k) * 3 + l]] = c.ddw(i, j, k, l);
+    });
+}
+
+// Model::Solid::Elastic::NeoHookean::W / DW / DDW (src/Model/Solid/Elastic/NeoHookean.H:19-66) at
+// n deformation gradients F (row-major 3 x 3 each): w[n], dw[n][9] row-major, ddw[n][45] the
+// Sym::Major slots, each read through the tensor's own (i, j, k, l) accessor at its
+// upper-triangle index (3i+j <= 3k+l)
+int ref_neohookean(double mu, double kappa, int n, const double* F, double* w, double* dw, double* ddw) {
+    return guarded([&] {
+        Model::Solid::Elastic::NeoHookean m;
+        m.mu = mu;
+        m.kappa = kappa;
+        for (int p = 0; p < n; p++) {
+            Set::Matrix Fm;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) Fm(i, j) = F[9 * p + 3 * i + j];
+            w[p] = m.W(Fm);
+            const Set::Matrix d = m.DW(Fm);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) dw[9 * p + 3 * i + j] = d(i, j);
+            const Set::Matrix4<3, Set::Sym::Major> t = m.DDW(Fm);
+            int s = 0;
+            for (int I = 0; I < 9; I++)
+                for (int K = I; K < 9; K++, s++) ddw[45 * p + s] = t(I / 3, I % 3, K / 3, K % 3);
+        }
     });
 }
 

@@ -23,6 +23,13 @@ Cases (inputs are multiples of 1/64, or of 1/1024 for the cubic tables: exact an
   fields         strain, strain_voigt (model-free), restrict, interp, bc_init, bc_init_homog on
                  the box level
   cubic          Linear::Cubic::Define(1.68, 1.21, 0.75, R) for 6 rotations: cubic_R, cubic_tabs
+  <lname>_major  the 45-slot Sym::Major kind (Elastic<Model::Solid::Elastic::NeoHookean>), its
+                 per-node tangent DDW(F) from the reference's NeoHookean at F = I + (multiples of
+                 1/64 in [-1/8, 1/8)), mu = 1.25, kappa = 2.5, rounded to multiples of 1/1024
+                 (a tangent field with the major symmetry only): the cases above without
+                 Stress / Energy (which read a linear model)
+  neo            NeoHookean::W / DW / DDW (mu = 1.3, kappa = 2.7) at 48 deformation gradients:
+                 neo_F, neo_w, neo_dw, neo_ddw (45 slots)
 
 Regenerate with:  python tests/golden/make_ref_golden.py
 """
@@ -43,7 +50,7 @@ OUT = os.path.join(HERE, "ref_ops.npz")
 CELLS = (8, 6, 10)
 DX = (0.1, 0.15, 0.08)
 D, T, N = 0, 1, 3
-NAMES = [(models.ISOTROPIC, "iso"), (models.MAJORMINOR, "mm"), (models.DIAGONAL, "diag")]
+NAMES = [(models.ISOTROPIC, "iso"), (models.MAJORMINOR, "mm"), (models.DIAGONAL, "diag"), (models.MAJOR, "major")]
 
 
 def q(rng, shape, lo=-64, hi=64):
@@ -58,6 +65,12 @@ def coeffs(model, shape, rng):
         return C, {"C": C}
     if model == models.DIAGONAL:
         C = np.ascontiguousarray(0.5 + q(rng, (9,) + shape, 0, 64))
+        return C, {"C": C}
+    if model == models.MAJOR:
+        from oracle.refshim import pyref
+        F = np.eye(3) + q(rng, shape + (3, 3), -8, 8)
+        ddw = pyref.neohookean(1.25, 2.5, F)[2].reshape(shape + (45,))
+        C = np.ascontiguousarray(np.moveaxis(np.round(ddw * 1024.0) / 1024.0, -1, 0))
         return C, {"C": C}
     Rs = models.random_rotations(4, rng)
     tabs = np.round(models.cubic(1.68, 1.21, 0.75, Rs) * 1024.0) / 1024.0
@@ -101,10 +114,11 @@ def make():
             if lname == "box":
                 Lc = po.coarsen(L)
                 out.update({p + "fapply_uniform": pyref.fapply(L, model, C, bt, u, True, bcval=bv),
-                            p + "stress": pyref.fields(L, model, C, "stress", u),
-                            p + "stress_voigt": pyref.fields(L, model, C, "stress", u, True),
-                            p + "energy": pyref.fields(L, model, C, "energy", u),
                             p + "coarse_C": pyref.average_down_coeffs(L, Lc, model, C)})
+                if model != models.MAJOR:
+                    out.update({p + "stress": pyref.fields(L, model, C, "stress", u),
+                                p + "stress_voigt": pyref.fields(L, model, C, "stress", u, True),
+                                p + "energy": pyref.fields(L, model, C, "energy", u)})
     rng = np.random.default_rng(3100)
     L = Ls["box"]
     Lc = po.coarsen(L)
@@ -123,6 +137,9 @@ def make():
     Rs = models.random_rotations(6, np.random.default_rng(3200))
     out["cubic_R"] = Rs
     out["cubic_tabs"] = np.stack([pyref.cubic_define(1.68, 1.21, 0.75, R) for R in Rs])
+    F = np.eye(3) + 0.25 * np.random.default_rng(3300).standard_normal((48, 3, 3))
+    w, dw, ddw = pyref.neohookean(1.3, 2.7, F)
+    out.update({"neo_F": F, "neo_w": w, "neo_dw": dw, "neo_ddw": ddw})
     return out
 
 

@@ -7,5 +7,7 @@ template class Operator::Elastic<Model::Solid::Linear::Cubic>;
 template class Operator::Elastic<Model::Solid::Linear::Laplacian>;
 template class Solver::Nonlocal::Newton<Model::Solid::Linear::Isotropic>;
 template class Solver::Nonlocal::Newton<Model::Solid::Linear::Cubic>;
+template class Operator::Elastic<Model::Solid::Elastic::NeoHookean>;
+template class Solver::Nonlocal::Newton<Model::Solid::Elastic::NeoHookean>;
 
 int main() { return 0; }

@@ -84,7 +84,7 @@ def _levels(*descs):
 
 
 @pytest.mark.parametrize("descs,model,what", [
-    ([(8, 0, 8, 0.125)], 3, b"model"),                                   # unknown stiffness kind
+    ([(8, 0, 8, 0.125)], 4, b"model"),                                   # unknown stiffness kind
     ([(8, 0, 8, 0.0)], 0, b"dx"),                                        # non-positive spacing
     ([(8, 0, 9, 0.125)], 0, b"outside"),                                 # patch beyond the domain
     ([(8, 2, 8, 0.125)], 0, b"whole domain"),                            # level 0 must cover it
