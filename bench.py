@@ -941,6 +941,9 @@ def main():
     ap.add_argument("--damage-floor", type=float, default=0.1,
                     help="stiffness floor of g(c) in the damaged workload (the specified 1e-6 diverges)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cell workload")
+    ap.add_argument("--no-neohookean", action="store_true", help="skip the NeoHookean Newton workload")
+    ap.add_argument("--neo-cells", type=int, default=96)
+    ap.add_argument("--neo-nriters", type=int, default=4)
     ap.add_argument("--no-serve", action="store_true", help="skip the served-cell workload")
     ap.add_argument("--no-builders", action="store_true",
                     help="skip timing the device-side model builders (mixture, degradation)")
@@ -1322,6 +1325,96 @@ def add_cell_workloads(args, lib, line, rank, world):
             line["model_builders"] = bench_model_builders(args)
         except Exception as e:  # pragma: no cover
             line["model_builders"] = {"error": str(e)}
+    if not args.no_neohookean:
+        try:
+            line["neohookean"] = bench_neohookean(args)
+        except Exception as e:  # pragma: no cover
+            line["neohookean"] = {"error": str(e)}
+
+
+def bench_neohookean(args):
+    """Newton<NeoHookean> (finite kinematics, the 45-slot Sym::Major tangent) on a box of
+    (cells)^3 cells: mu 1, kappa 2.5, symmetry rollers on the low faces, x = 1 pulled by 5 %, a
+    smooth body force; nriters Newton iterations from u = 0, each one ae_newton_neohookean (the
+    tangent DDW(I + grad u) and rhs = b - N(u)) and one Linear solve of the correction to 1e-10.
+    Device time per Newton solve in FP64 and mixed precision, the end-to-end time through host
+    buffers, the Newton residual max|b - N(u)| / max|b| left after the last iteration, and the
+    FP32 tangent Jacobi sweep (228 algorithmic B per node: 45 slots + x, b, 1/D, out) timed alone."""
+    import ctypes as C
+    import torch
+    from anisotropicfracture_gb300 import _lib, models
+    from anisotropicfracture_gb300.elastic import FACES, BCElastic, Elastic, Field, Newton, level_desc
+    from oracle import pyoracle as po
+    n = args.neo_cells
+    neo = models.NeoHookean(1.0, 2.5)
+    bc = BCElastic()
+    for f, name in enumerate(FACES):
+        for p, ax in enumerate("XYZ"):
+            bc.type[f, p] = bc.Traction
+            if ax + "LO" in name:
+                bc.type[f, p] = bc.Displacement
+            elif ax == "X" and "XHI" in name:
+                bc.type[f, p], bc.val[f, p] = bc.Displacement, 0.05
+    L = po.level(n)
+    X, Y, Z = po.node_coords(L)
+    force = np.zeros((3,) + L.shape)
+    force[1] = 0.05 * np.sin(np.pi * X) * np.sin(np.pi * Z)
+    b = po.bc_init(L, bc.type, bc.val, force)
+    op = Elastic([level_desc(n)], models.MAJOR)
+    op.SetBC(bc)
+    op.SetUniform(False)  # the operator's own stream, ordered with the legacy default stream
+    s = Newton(op)
+    s.setNRIters(args.neo_nriters)
+    s.setMaxFmgIter(0)
+    s.setBottomSolver("bicgstab")
+    s.setPreSmooth(2)
+    s.setPostSmooth(2)
+    s.opts.max_iter = 400
+    bd = torch.from_numpy(b).cuda()
+    out = {"workload": "%d^3 cells NeoHookean (mu 1, kappa 2.5), x = 1 pulled 5 %%, rollers on the low faces, "
+                       "body force 0.05 sin(pi x) sin(pi z) e_y, %d Newton iterations, V(2,2) + BiCGStab, "
+                       "corrections to tol_rel 1e-10" % (n, args.neo_nriters), "unit": "newton solves/s"}
+    for prec, inner in (("fp64", 1), ("mixed", 4)):
+        s.setPrecision(prec)
+        s.opts.inner_cycles = inner
+        ud = torch.zeros_like(bd)
+
+        def one():
+            ud.zero_()
+            s.solve(Field(ud), Field(bd), model=neo, tol_rel=1e-10, tol_abs=0.0)
+
+        one()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        one()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        rec = {"value": 1000.0 / ms, "ms_per_newton_solve": ms, "mg_iters_last": s.stats.iters,
+               "inner_cycles": inner}
+        rd = bd.clone()
+        op.NewtonNeoHookean(0, Field(rd), Field(ud), Field(bd), neo)
+        torch.cuda.synchronize()
+        rec["newton_residual"] = float(rd.abs().max()) / float(bd.abs().max())
+        uh = np.zeros_like(b)
+        t0 = time.perf_counter()
+        s.solve(Field(uh), Field(b), model=neo, tol_rel=1e-10, tol_abs=0.0)
+        e2e = time.perf_counter() - t0
+        rec["e2e"] = {"value": 1.0 / e2e, "unit": "newton solves/s", "h2d_bytes_per_step": 2 * b.nbytes,
+                      "d2h_bytes_per_step": b.nbytes}
+        rec["e2e_vs_device_max_abs_diff"] = float(np.abs(uh - ud.cpu().numpy()).max())
+        out[prec] = rec
+    ms = C.c_double(0.0)
+    lib = _lib.load()
+    _lib.check(lib.ae_profile_kernel(op.handle, 1, 0, 0, 1, 20, C.byref(ms)))
+    nodes = (n + 1) ** 3
+    gbs = 228.0 * nodes / (ms.value * 1e-3) / 1e9
+    peak, kind = measured_peaks()
+    out["tangent_jacobi_fp32"] = {"ms": ms.value, "bytes_per_node": 228, "GB/s": gbs, "frac": gbs / peak,
+                                  "peak": kind}
+    op.close()
+    return out
 
 
 def bench_model_builders(args, reps=5):
