@@ -200,6 +200,9 @@ void CellEngine::invalidate_graphs() {
         if (gexec[p]) cudaGraphExecDestroy(gexec[p]);
         gexec[p] = nullptr;
         gvalid[p] = false;
+        if (wexec[p]) cudaGraphExecDestroy(wexec[p]);
+        wexec[p] = nullptr;
+        wvalid[p] = false;
     }
 }
 
@@ -550,6 +553,69 @@ void CellEngine::iterate(int prec, const ae_solver_opts& o, double tol_rel, doub
     g_kernel_launches.fetch_add(glaunches[prec]);
 }
 
+bool CellEngine::iterate_all(int prec, const ae_solver_opts& o, double tol_rel, double tol_abs) {
+    if (!o.use_graph || !while_ok) return false;
+    ae_solver_opts key = o;
+    key.max_fmg_iter = 0;
+    if (wvalid[prec] && (!same_opts(wopts[prec], key) || wtol[prec][0] != tol_rel || wtol[prec][1] != tol_abs)) {
+        cudaGraphExecDestroy(wexec[prec]);
+        wexec[prec] = nullptr;
+        wvalid[prec] = false;
+    }
+    if (!wvalid[prec]) {
+        cudaGraph_t g = nullptr;
+        AEH_CHECK(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle h;
+        cudaGraphNodeParams np = {};
+        cudaGraphNode_t node;
+        if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphDestroy(g);
+            while_ok = false;
+            return false;
+        }
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphDestroy(g);
+            while_ok = false;
+            return false;
+        }
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        const long long before = g_kernel_launches.load();
+        AEH_CHECK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+            iteration_body(prec, o, tol_rel, tol_abs);
+            cells_launch_loop_cond(h, dcount, dcount + 1, o.max_iter + 2, st);
+        } catch (...) {
+            cudaGraph_t tmp = nullptr;
+            cudaStreamEndCapture(st, &tmp);
+            cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t captured = nullptr;
+        AEH_CHECK(cudaStreamEndCapture(st, &captured));
+        const cudaError_t e = cudaGraphInstantiate(&wexec[prec], g, 0);
+        cudaGraphDestroy(g);
+        AEH_CHECK(e);
+        wlaunches[prec] = g_kernel_launches.load() - before;
+        g_kernel_launches.fetch_sub(wlaunches[prec]);
+        wopts[prec] = key;
+        wtol[prec][0] = tol_rel;
+        wtol[prec][1] = tol_abs;
+        wvalid[prec] = true;
+    }
+    AEH_CHECK(cudaMemsetAsync(dcount + 1, 0, sizeof(int), st));
+    AEH_CHECK(cudaGraphLaunch(wexec[prec], st));
+    AEH_CHECK(cudaMemcpyAsync(hcount + 1, dcount + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AEH_CHECK(cudaStreamSynchronize(st));
+    g_kernel_launches.fetch_add(wlaunches[prec] * hcount[1]);
+    return true;
+}
+
 int CellEngine::read_count() {
     AEH_CHECK(cudaMemcpyAsync(hcount, dcount, sizeof(int), cudaMemcpyDeviceToHost, st));
     AEH_CHECK(cudaStreamSynchronize(st));
@@ -807,7 +873,11 @@ int ae_batch_solve(ae_batch b, double tol_rel, double tol_abs, const ae_solver_o
         // the tuner times smoother sweeps that write only the second correction buffers, which
         // the first sweep of every V-cycle overwrites
         if (!E.tuned[prec] && count > 0) E.tune(prec, o);
-        for (int it = 0; count > 0 && it <= o.max_iter + 1; ++it) {
+        // the whole iteration sequence as one graph launch (a device-side WHILE loop); the
+        // host-polled replay where the runtime has no conditional nodes or graphs are off
+        const bool whole = count > 0 && E.iterate_all(prec, o, tol_rel, tol_abs);
+        if (whole) count = E.read_count();
+        for (int it = 0; !whole && count > 0 && it <= o.max_iter + 1; ++it) {
             E.iterate(prec, o, tol_rel, tol_abs);
             count = E.read_count();
         }

@@ -135,6 +135,8 @@ void cells_launch_stress(int model, const CellArgs& A, const Work* tab, int ntab
 // active_out (optional, one int per visited solve) their flags
 void cells_launch_status(const CellArgs& A, const int* slots, int nsolves, int first, double tol_rel, double tol_abs,
                          int max_iter, int* count, int* active_out, cudaStream_t st);
+// *iter += 1; the WHILE node's condition = (*count > 0 && *iter < limit)
+void cells_launch_loop_cond(cudaGraphConditionalHandle h, const int* count, int* iter, int limit, cudaStream_t st);
 void cells_launch_begin(const CellArgs& A, const int* slots, int nsolves, cudaStream_t st);
 void cells_launch_zero_x(const CellArgs& A, const Work* tab, int ntab, cudaStream_t st);
 // cell set-up (tab over cell ids): C_{m} = R C_{m-1}; D, 1/D, FP32 copies; NaN flag

@@ -87,6 +87,14 @@ struct CellEngine {
     ae_solver_opts gopts[2];
     double gtol[2][2] = {{0, 0}, {0, 0}};
     bool gvalid[2] = {false, false};
+    // one graph per precision that runs the whole iteration sequence: a conditional WHILE node
+    // whose body is the iteration and the loop condition (dcount[1] counts the iterations)
+    cudaGraphExec_t wexec[2] = {nullptr, nullptr};
+    long long wlaunches[2] = {0, 0};
+    ae_solver_opts wopts[2];
+    double wtol[2][2] = {{0, 0}, {0, 0}};
+    bool wvalid[2] = {false, false};
+    bool while_ok = true;  // false once the runtime refused a conditional node
 
     explicit CellEngine(int model);
     ~CellEngine();
@@ -113,6 +121,9 @@ struct CellEngine {
     void vcycle(int prec, const ae_solver_opts& o);
     void iteration_body(int prec, const ae_solver_opts& o, double tol_rel, double tol_abs);
     void iterate(int prec, const ae_solver_opts& o, double tol_rel, double tol_abs);  // graph or direct
+    // every iteration until no solve is active (or max_iter + 2 of them) in one graph launch;
+    // false (nothing run) when graphs are off or the runtime has no conditional nodes
+    bool iterate_all(int prec, const ae_solver_opts& o, double tol_rel, double tol_abs);
     int read_count();
     // per-slot active flags of the last iteration (host copy, valid after read_active)
     const int* read_active();

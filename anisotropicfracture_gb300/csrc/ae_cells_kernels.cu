@@ -613,6 +613,14 @@ __global__ void __launch_bounds__(1024) kb_status(CellArgs A, const int* slots, 
     if (threadIdx.x == 0) *count = total;
 }
 
+// Loop condition of the batch's device-side iteration (the body of a conditional WHILE graph
+// node): continue while some solve is active and fewer than `limit` iterations have run.  The
+// counter bounds the loop whatever the status says.
+__global__ void kb_loop_cond(cudaGraphConditionalHandle h, const int* count, int* iter, int limit) {
+    const int it = *iter + 1;
+    *iter = it;
+    cudaGraphSetConditional(h, (*count > 0 && it < limit) ? 1u : 0u);
+}
 // ------------------------------------------------------------------ cell set-up
 template <int M>
 __global__ void __launch_bounds__(kCellThreads) kb_coarsen_C(CellArgs A, const Work* __restrict__ tab, int ntab,
@@ -861,6 +869,11 @@ void cells_launch_diag(int model, const CellArgs& A, const Work* tab, int ntab, 
     dispatch_model<double>(model, [&](auto mm) {
         kb_diag<decltype(mm)::value><<<ntab, kRedChunk, 0, st>>>(A, tab, ntab, m, nan_flag);
     });
+    launched();
+}
+
+void cells_launch_loop_cond(cudaGraphConditionalHandle h, const int* count, int* iter, int limit, cudaStream_t st) {
+    kb_loop_cond<<<1, 1, 0, st>>>(h, count, iter, limit);
     launched();
 }
 

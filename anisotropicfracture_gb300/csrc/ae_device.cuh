@@ -51,6 +51,7 @@ struct View {
     T* p;
     int lo[3];
     long long sy, sz, sc;
+    int wx = 0;  // nodes per row when the row pitch sy is padded past them (0: sy)
     __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
         return (long long)(i - lo[0]) + (long long)(j - lo[1]) * sy + (long long)(k - lo[2]) * sz;
     }

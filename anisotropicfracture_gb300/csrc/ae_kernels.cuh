@@ -647,11 +647,26 @@ __global__ void __launch_bounds__(kBlock) k_flat_axpy(long long n, Ro* __restric
         else dst[t] += (Ro)(alpha * (double)src[t]);
     }
 }
-// true when region, taken over ncomp components, is exactly the contiguous storage of v
+// true when region, taken over ncomp components, covers whole rows and planes of v's storage
+// from its first node, so that the elements from there on form one contiguous run (row padding
+// included: padding is never read by the stencil kernels, and the level arrays hold it)
 template <class T>
 inline bool flat_view(const Reg& reg, int ncomp, const View<T>& v) {
+    const long long w = v.wx > 0 ? v.wx : v.sy;
+    const long long ny = reg.nxy / reg.nx, nz = reg.n / reg.nxy;
     return reg.n > 0 && reg.lo[0] == v.lo[0] && reg.lo[1] == v.lo[1] && reg.lo[2] == v.lo[2] &&
-           (long long)reg.nx == v.sy && (long long)reg.nxy == v.sz && (ncomp == 1 || (long long)reg.n == v.sc);
+           (long long)reg.nx == w && ny * v.sy == v.sz && (ncomp == 1 || nz * v.sz == v.sc);
+}
+// elements of that contiguous run
+template <class T>
+inline long long flat_count(const Reg& reg, int ncomp, const View<T>& v) {
+    const long long nz = reg.n / reg.nxy;
+    return ncomp == 1 ? nz * v.sz : v.sc * ncomp;
+}
+// the same run in two views: same pitches
+template <class A, class B>
+inline bool same_pitch(const View<A>& a, const View<B>& b) {
+    return a.sy == b.sy && a.sz == b.sz && a.sc == b.sc;
 }
 // grid of a flat loop: enough blocks to cover n, capped at 8 resident blocks per SM of 152
 inline unsigned flat_blocks(long long n) {

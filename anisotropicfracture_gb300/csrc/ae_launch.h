@@ -78,6 +78,7 @@ View<T> level_view(const Geo& g, T* p) {
     v.sy = g.px > 0 ? g.px : s.hi[0] - s.lo[0] + 1;
     v.sz = v.sy * (s.hi[1] - s.lo[1] + 1);
     v.sc = v.sz * (s.hi[2] - s.lo[2] + 1);
+    v.wx = s.hi[0] - s.lo[0] + 1;
     return v;
 }
 // elements per component of a level's internal arrays (padding included)
@@ -93,6 +94,7 @@ View<const T> cview(const View<T>& v) {
     c.p = v.p;
     for (int d = 0; d < 3; ++d) c.lo[d] = v.lo[d];
     c.sy = v.sy; c.sz = v.sz; c.sc = v.sc;
+    c.wx = v.wx;
     return c;
 }
 
