@@ -110,6 +110,8 @@ struct MGLevel {
 
 struct AmrLevel {
     ae_level_desc desc;
+    int rl = 0;       // refinement level (0: the base level)
+    int parent = -1;  // the patch of level rl - 1 this patch nests in
     std::vector<MGLevel> mg;
     double *sol = nullptr, *rhs = nullptr;
     float *sol32 = nullptr, *rhs32 = nullptr;  // mixed precision: correction and its right-hand side
@@ -124,7 +126,8 @@ struct ae_op_s {
     double bcval[26 * 3];
     bool bc_set = false;
     int uniform = 0, homogeneous = 0;
-    std::vector<AmrLevel> amr;
+    std::vector<AmrLevel> amr;               // the patches, level by level (entry 0: the base level)
+    std::vector<std::vector<int>> rlev;      // the patches of each refinement level
     cudaStream_t st = nullptr;
     cudaStream_t own_st = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -664,23 +667,28 @@ struct AmrIter {
     cudaStream_t st;
     std::vector<R*> sol, rhs;  // per AMR level, level storage layout
 
-    int finest() const { return (int)op->amr.size() - 1; }
+    int finest() const { return (int)op->amr.size() - 1; }  // last patch
+    int top() const { return (int)op->rlev.size() - 1; }    // finest refinement level
+    const std::vector<int>& lev(int r) const { return op->rlev[r]; }
+    int up(int a) const { return op->amr[a].parent; }
     MGLevel& T(int a) { return op->amr[a].mg[0]; }
     const Geo& G(int a) { return T(a).g; }
     LevelPtrs<R> P(int a) { return ptrs<R>(T(a)); }
     View<R> V(int a, R* p) { return level_view(G(a), p); }
     View<const R> CV(int a, R* p) { return cview(level_view(G(a), p)); }
     Box3 store_dom(int a) { return box_isect(geo_store(G(a)), geo_domain(G(a))); }
-    Box3 covered(int a) {  // coarse nodes of level a-1 under the patch of level a
+    Box3 covered(int a) {  // nodes of the parent patch under patch a
         Box3 b;
         for (int d = 0; d < 3; ++d) { b.lo[d] = G(a).vlo[d] / 2; b.hi[d] = G(a).vhi[d] / 2; }
-        return box_isect(b, geo_domain(G(a - 1)));
+        return box_isect(b, geo_domain(G(up(a))));
     }
     void sol_residual(int a) { sweep_residual<R>(op, G(a), P(a).C, sol[a], rhs[a], P(a).res, st); }
     void cor_residual(int a) { sweep_residual<R>(op, G(a), P(a).C, P(a).cor, P(a).res, P(a).res, st); }  // in place
-    void reflux(int c) {
-        const Box3 r = covered(c + 1);
-        launch_restrict<R>(G(c), 3, V(c, P(c).res), CV(c + 1, P(c + 1).res), st, &r);
+    // the residual of patch e restricted onto the nodes of its parent it covers
+    void reflux(int e) {
+        const int c = up(e);
+        const Box3 r = covered(e);
+        launch_restrict<R>(G(c), 3, V(c, P(c).res), CV(e, P(e).res), st, &r);
     }
     void add_cor(int a) { launch_axpy<R, R>(store_dom(a), 3, V(a, sol[a]), 1.0, CV(a, P(a).cor), st); }
     void mini_cycle(int a) {
@@ -691,39 +699,46 @@ struct AmrIter {
     void interp_cor(int a) {
         launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
         const Box3 r = store_dom(a);
-        launch_interp_add<R>(G(a), 3, V(a, P(a).cor), CV(a - 1, P(a - 1).cor), st, &r);
+        launch_interp_add<R>(G(a), 3, V(a, P(a).cor), CV(up(a), P(up(a)).cor), st, &r);
     }
-    void average_down(int a) { launch_inject<R>(covered(a), 3, V(a - 1, sol[a - 1]), CV(a, sol[a]), st); }
-    // residual of every level, fine residuals refluxed onto covered coarse nodes
+    void average_down(int a) { launch_inject<R>(covered(a), 3, V(up(a), sol[up(a)]), CV(a, sol[a]), st); }
+    // residual of every level, fine residuals refluxed onto covered coarse nodes (level by level,
+    // finest first; the patches of a level are independent)
     void ml_residual() {
-        for (int a = finest(); a >= 0; --a) {
-            sol_residual(a);
-            if (a < finest()) reflux(a);
+        for (int r = top(); r >= 0; --r) {
+            for (int a : lev(r)) sol_residual(a);
+            if (r < top())
+                for (int e : lev(r + 1)) reflux(e);
         }
     }
     void one_iter(bool fcyc) {
-        const int F = finest();
-        for (int a = F; a >= 1; --a) {
-            mini_cycle(a);
-            add_cor(a);
-            sol_residual(a - 1);  // computeResWithCrseSolFineCor
-            cor_residual(a);
-            reflux(a - 1);
-            if (a != F) launch_copy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), CV(a, P(a).cor), st);
+        const int F = top();
+        for (int r = F; r >= 1; --r) {
+            for (int a : lev(r)) {
+                mini_cycle(a);
+                add_cor(a);
+            }
+            for (int c : lev(r - 1)) sol_residual(c);  // computeResWithCrseSolFineCor
+            for (int a : lev(r)) {
+                cor_residual(a);
+                reflux(a);
+                if (r != F) launch_copy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), CV(a, P(a).cor), st);
+            }
         }
         Cycle<R> cy{op, o, op->amr[0].mg, st};
         cy.run(fcyc);
         add_cor(0);
-        for (int a = 1; a <= F; ++a) {
-            interp_cor(a);
-            add_cor(a);
-            if (a != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), 1.0, CV(a, P(a).cor), st);
-            cor_residual(a);  // computeResWithCrseCorFineCor
-            mini_cycle(a);
-            add_cor(a);
-            if (a != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).cor), 1.0, CV(a, P(a).corhold), st);
-        }
-        for (int a = F; a >= 1; --a) average_down(a);
+        for (int r = 1; r <= F; ++r)
+            for (int a : lev(r)) {
+                interp_cor(a);
+                add_cor(a);
+                if (r != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).corhold), 1.0, CV(a, P(a).cor), st);
+                cor_residual(a);  // computeResWithCrseCorFineCor
+                mini_cycle(a);
+                add_cor(a);
+                if (r != F) launch_axpy<R, R>(geo_store(G(a)), 3, V(a, P(a).cor), 1.0, CV(a, P(a).corhold), st);
+            }
+        for (int a = finest(); a >= 1; --a) average_down(a);  // entries run level by level
     }
 };
 
@@ -801,7 +816,7 @@ void iteration_body(ae_op* op, const ae_solver_opts& o, bool fcyc) {
             // the patches' outermost ghost rings: the coarse correction interpolated in FP64, as
             // the FP64 solve's rings hold (see k_ring_interp_fix)
             for (int a = 1; a <= it.finest(); ++a)
-                launch_ring_interp_fix(it.G(a), level_view(it.G(a), op->amr[a].sol), it.CV(a - 1, e[a - 1]),
+                launch_ring_interp_fix(it.G(a), level_view(it.G(a), op->amr[a].sol), it.CV(it.up(a), e[it.up(a)]),
                                        it.CV(a, e[a]), st);
             AmrIter<double> it64{op, o, st, sol64(op), rhs64(op)};
             for (int a = it.finest(); a >= 1; --a) it64.average_down(a);
@@ -982,12 +997,37 @@ int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) 
                 g.vlo[d] = L.lo[d];
                 g.vhi[d] = L.hi[d];
                 g.dx[d] = L.dx[d];
-                if (a > 0) {
-                    const ae_level_desc& Pc = levels[a - 1];
-                    require(L.domain_cells[d] == 2 * Pc.domain_cells[d], "AMR levels must refine by 2");
-                    require(L.lo[d] % 2 == 0 && L.hi[d] % 2 == 0, "fine patch must align with coarse nodes");
-                    require(L.lo[d] / 2 >= Pc.lo[d] && L.hi[d] / 2 <= Pc.hi[d], "fine patch must nest in the coarse patch");
+                if (a > 0) require(L.lo[d] % 2 == 0 && L.hi[d] % 2 == 0, "fine patch must align with coarse nodes");
+            }
+            // the hierarchy: consecutive entries with one domain are the patches of one level; a
+            // new level refines the previous one by 2 and each patch nests in one patch below it
+            if (a == 0) {
+                op->rlev.assign(1, std::vector<int>{0});
+            } else {
+                const ae_level_desc& Pv = levels[a - 1];
+                bool same = true, twice = true;
+                for (int d = 0; d < 3; ++d) {
+                    same = same && L.domain_cells[d] == Pv.domain_cells[d];
+                    twice = twice && L.domain_cells[d] == 2 * Pv.domain_cells[d];
                 }
+                require((same && op->amr[a - 1].rl >= 1) || twice, "AMR levels must refine by 2");
+                A.rl = same && op->amr[a - 1].rl >= 1 ? op->amr[a - 1].rl : op->amr[a - 1].rl + 1;
+                if (A.rl == (int)op->rlev.size()) op->rlev.emplace_back();
+                for (int q : op->rlev[A.rl - 1]) {
+                    const ae_level_desc& Pc = levels[q];
+                    bool in = true;
+                    for (int d = 0; d < 3; ++d) in = in && L.lo[d] / 2 >= Pc.lo[d] && L.hi[d] / 2 <= Pc.hi[d];
+                    if (in) { A.parent = q; break; }
+                }
+                require(A.parent >= 0, "fine patch must nest in a patch of the coarser level");
+                for (int q : op->rlev[A.rl]) {  // storage boxes grow(valid, 2) of one level disjoint
+                    const ae_level_desc& Pq = levels[q];
+                    bool apart = false;
+                    for (int d = 0; d < 3; ++d)
+                        apart = apart || L.lo[d] - 2 > Pq.hi[d] + 2 || Pq.lo[d] - 2 > L.hi[d] + 2;
+                    require(apart, "patches of one level must be separated (their ghost layers may not meet)");
+                }
+                op->rlev[A.rl].push_back(a);
             }
             if (a == 0) {
                 for (int d = 0; d < 3; ++d)

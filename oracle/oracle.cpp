@@ -677,9 +677,59 @@ Box covered_by(const Lev& Lf) {
     return b;
 }
 
+// The AMR hierarchy as a list of patches: entry 0 covers the level-0 domain; the entries of a
+// finer level follow, with twice the domain of the level before.  Several entries with one
+// domain are the patches of one level (an AMReX BoxArray of separated boxes: their storage boxes
+// grow(valid, 2) are disjoint, so no ghost node of one patch lies in another, and AMReX's
+// FillBoundary between them has nothing to copy).  Each patch nests in one patch of the level
+// below, its parent.  Returns false when the list does not describe such a hierarchy.
+struct Hier {
+    std::vector<int> rl, parent;     // refinement level and parent entry of every entry
+    std::vector<std::vector<int>> at;  // the entries of each level
+    int R = 0;                         // finest level
+    bool build(const orc_level* Ls, int n) {
+        rl.assign(n, 0);
+        parent.assign(n, -1);
+        at.assign(1, std::vector<int>{0});
+        for (int a = 1; a < n; ++a) {
+            bool same = true, twice = true;
+            for (int d = 0; d < 3; ++d) {
+                same = same && Ls[a].dom_hi[d] == Ls[a - 1].dom_hi[d];
+                twice = twice && Ls[a].dom_hi[d] == 2 * Ls[a - 1].dom_hi[d];
+            }
+            if (same && a > 1 && rl[a - 1] >= 1) {
+                rl[a] = rl[a - 1];
+            } else if (twice) {
+                rl[a] = rl[a - 1] + 1;
+                at.emplace_back();
+            } else {
+                return false;
+            }
+            at[rl[a]].push_back(a);
+            for (int q : at[rl[a] - 1]) {
+                bool in = true;
+                for (int d = 0; d < 3; ++d)
+                    in = in && Ls[a].lo[d] / 2 >= Ls[q].lo[d] && Ls[a].hi[d] / 2 <= Ls[q].hi[d];
+                if (in) { parent[a] = q; break; }
+            }
+            if (parent[a] < 0) return false;
+            for (int q : at[rl[a]]) {  // separated from the level's other patches
+                if (q == a) continue;
+                bool apart = false;
+                for (int d = 0; d < 3; ++d)
+                    apart = apart || Ls[a].lo[d] - 2 > Ls[q].hi[d] + 2 || Ls[q].lo[d] - 2 > Ls[a].hi[d] + 2;
+                if (!apart) return false;
+            }
+        }
+        R = (int)at.size() - 1;
+        return true;
+    }
+};
+
 struct Amr {
     Solver* S = nullptr;
     std::vector<FineLevel> F;
+    Hier H;
     double* sol0 = nullptr;
     const double* rhs0 = nullptr;
     int finest() const { return (int)F.size(); }
@@ -709,7 +759,11 @@ struct Amr {
                 f.res[c] = f.rescor[c];
             });
     }
-    void reflux(int c) { restrict_box(L(c), L(c + 1), 3, res(c), res(c + 1), isect(covered_by(L(c + 1)), L(c).dom)); }
+    // the fine residual of patch e restricted onto the coarse nodes of its parent it covers
+    void reflux(int e) {
+        const int c = H.parent[e];
+        restrict_box(L(c), L(e), 3, res(c), res(e), isect(covered_by(L(e)), L(c).dom));
+    }
     void add(int a, const double* x) {
         double* s = sol(a);
         for (long i = 0; i < N(a); ++i) s[i] += x[i];
@@ -717,13 +771,13 @@ struct Amr {
     void interp_cor(int a) {
         FineLevel& f = F[a - 1];
         std::fill(f.cor.begin(), f.cor.end(), 0.0);
-        interp_add_box(*f.L, L(a - 1), 3, f.cor.data(), cor(a - 1), isect(f.L->store, f.L->dom));
+        interp_add_box(*f.L, L(H.parent[a]), 3, f.cor.data(), cor(H.parent[a]), isect(f.L->store, f.L->dom));
     }
     void average_down(int a) {
-        Lev& Lc = L(a - 1);
+        Lev& Lc = L(H.parent[a]);
         Lev& Lf = L(a);
         const Box r = isect(covered_by(Lf), Lc.dom);
-        double* sc = sol(a - 1);
+        double* sc = sol(H.parent[a]);
         const double* sf = sol(a);
         for (int n = 0; n < 3; ++n)
             for_box(r, [&](int I, int J, int K) {
@@ -740,41 +794,49 @@ struct Amr {
                     for (int i = r.lo[0]; i <= r.hi[0]; ++i) m = amax(m, v[n * l.nn + l.at(i, j, k)]);
         return m;
     }
-    // MLMG::computeMLResidual + composite max-norm
+    // MLMG::computeMLResidual + composite max-norm (level by level, finest first; the patches of
+    // a level are independent)
     double ml_residual() {
         double m = 0;
-        for (int a = finest(); a >= 0; --a) {
-            sol_residual(a);
-            if (a < finest()) reflux(a);
+        for (int r = H.R; r >= 0; --r) {
+            for (int e : H.at[r]) sol_residual(e);
+            if (r < H.R)
+                for (int e : H.at[r + 1]) reflux(e);
         }
         for (int a = 0; a <= finest(); ++a) m = std::max(m, norm(a, res(a)));
         return m;
     }
     void one_iter(int it) {
-        for (int a = finest(); a >= 1; --a) {
-            mini_cycle(a);
-            add(a, cor(a));
-            sol_residual(a - 1);  // computeResWithCrseSolFineCor
-            cor_residual(a);
-            reflux(a - 1);
-            if (a != finest()) F[a - 1].corhold = F[a - 1].cor;
+        for (int r = H.R; r >= 1; --r) {
+            for (int e : H.at[r]) {
+                mini_cycle(e);
+                add(e, cor(e));
+            }
+            for (int c : H.at[r - 1]) sol_residual(c);  // computeResWithCrseSolFineCor
+            for (int e : H.at[r]) {
+                cor_residual(e);
+                reflux(e);
+                if (r != H.R) F[e - 1].corhold = F[e - 1].cor;
+            }
         }
         if (it < S->o.max_fmg_iter) S->fcycle();
         else S->vcycle(0);
         add(0, cor(0));
-        for (int a = 1; a <= finest(); ++a) {
-            FineLevel& f = F[a - 1];
-            interp_cor(a);
-            add(a, cor(a));
-            if (a != finest())
-                for (size_t i = 0; i < f.cor.size(); ++i) f.corhold[i] += f.cor[i];
-            cor_residual(a);  // computeResWithCrseCorFineCor
-            mini_cycle(a);
-            add(a, cor(a));
-            if (a != finest())
-                for (size_t i = 0; i < f.cor.size(); ++i) f.cor[i] += f.corhold[i];
-        }
-        for (int a = finest(); a >= 1; --a) average_down(a);
+        for (int r = 1; r <= H.R; ++r)
+            for (int a : H.at[r]) {
+                FineLevel& f = F[a - 1];
+                interp_cor(a);
+                add(a, cor(a));
+                if (r != H.R)
+                    for (size_t i = 0; i < f.cor.size(); ++i) f.corhold[i] += f.cor[i];
+                cor_residual(a);  // computeResWithCrseCorFineCor
+                mini_cycle(a);
+                add(a, cor(a));
+                if (r != H.R)
+                    for (size_t i = 0; i < f.cor.size(); ++i) f.cor[i] += f.corhold[i];
+            }
+        for (int r = H.R; r >= 1; --r)
+            for (int a : H.at[r]) average_down(a);
     }
 };
 
@@ -997,6 +1059,8 @@ int orc_residual_amr(const orc_level* Ls, int namr, int model, const double* con
                      int uniform, const double* const* us, const double* const* bs, double* const* rs,
                      double* norm_inf) {
     if (namr < 1 || Ls[0].ng != 0) return -1;
+    Hier H;
+    if (!H.build(Ls, namr)) return -1;
     std::vector<std::unique_ptr<Lev>> L;
     std::vector<std::vector<double>> own(namr);
     std::vector<double*> r(namr);
@@ -1009,9 +1073,13 @@ int orc_residual_amr(const orc_level* Ls, int namr, int model, const double* con
             r[a] = own[a].data();
         }
     }
-    for (int a = namr - 1; a >= 0; --a) {
-        residual(*L[a], model, Cs[a], bctype, uniform, us[a], bs[a], r[a]);
-        if (a + 1 < namr) restrict_box(*L[a], *L[a + 1], 3, r[a], r[a + 1], isect(covered_by(*L[a + 1]), L[a]->dom));
+    for (int lv = H.R; lv >= 0; --lv) {
+        for (int a : H.at[lv]) residual(*L[a], model, Cs[a], bctype, uniform, us[a], bs[a], r[a]);
+        if (lv < H.R)
+            for (int e : H.at[lv + 1]) {
+                const int c = H.parent[e];
+                restrict_box(*L[c], *L[e], 3, r[c], r[e], isect(covered_by(*L[e]), L[c]->dom));
+            }
     }
     double m = 0.0;
     for (int a = 0; a < namr; ++a) {
@@ -1027,7 +1095,8 @@ int orc_residual_amr(const orc_level* Ls, int namr, int model, const double* con
 
 // MLMG::solve restated: convergence when the composite ||r||_inf <= max(tol_abs, tol_rel * max_norm),
 // max_norm = ||b||_inf if ||b||_inf >= ||r0||_inf else ||r0||_inf.  Ls[0] covers its domain
-// (ng = 0); Ls[l >= 1] are nested patches refined by 2 with ng = 2.
+// (ng = 0); Ls[l >= 1] are patches of finer levels refined by 2 with ng = 2, several per level
+// when they share a domain (Hier).
 int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
                   double* const* us, const double* const* bs, double tol_rel, double tol_abs, const orc_opts* opts,
                   orc_stats* stats) {
@@ -1068,6 +1137,7 @@ int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const*
     for (int m = 0; m < nlev; ++m) diagonal(*S.lv[m].L, model, S.lv[m].C.data(), bctype, S.lv[m].D.data());
 
     Amr A;
+    if (!A.H.build(Ls, namr)) return -1;
     A.S = &S;
     A.sol0 = u;
     A.rhs0 = b;

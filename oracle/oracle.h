@@ -92,8 +92,10 @@ void orc_mm_div(const double* c21, const double* b27, double* f3);
 int orc_solve(const orc_level* L, int model, const double* C, const int* bctype,
               double* u, const double* b, double tol_rel, double tol_abs,
               const orc_opts* opts, orc_stats* stats);
-/* composite multi-level solve: Ls[0] covers its domain (ng = 0); Ls[l >= 1] are nested
- * patches refined by 2 with ng = 2; Cs, us, bs hold one stored field per level */
+/* composite multi-level solve: Ls[0] covers its domain (ng = 0); Ls[l >= 1] are patches of finer
+ * levels refined by 2 with ng = 2, listed level by level; consecutive entries with one domain are
+ * the patches of one level (storage boxes grow(valid, 2) disjoint), each nested in one patch of
+ * the level below.  Cs, us, bs hold one stored field per entry.  -1 for a malformed list. */
 int orc_solve_amr(const orc_level* Ls, int namr, int model, const double* const* Cs, const int* bctype,
                   double* const* us, const double* const* bs, double tol_rel, double tol_abs,
                   const orc_opts* opts, orc_stats* stats);

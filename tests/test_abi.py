@@ -90,6 +90,8 @@ def _levels(*descs):
     ([(8, 2, 8, 0.125)], 0, b"whole domain"),                            # level 0 must cover it
     ([(8, 0, 8, 0.125), (12, 4, 8, 0.0625)], 0, b"refine by 2"),         # refinement ratio
     ([(8, 0, 8, 0.125), (16, 3, 9, 0.0625)], 0, b"align"),               # odd fine patch corners
+    ([(8, 0, 8, 0.125), (16, 2, 6, 0.0625), (16, 8, 12, 0.0625)], 0, b"separated"),  # patches' ghosts meet
+    ([(8, 0, 8, 0.125), (16, 2, 6, 0.0625), (32, 20, 28, 0.03125)], 0, b"nest"),    # no parent patch
 ])
 def test_level_descriptions_are_checked_on_the_host(lib, descs, model, what):
     """Operator::Elastic<T>::define's preconditions (src/Operator/Elastic.cpp:30-55) are checked
