@@ -128,7 +128,14 @@ const char* ae_version(void);
 void ae_default_solver_opts(ae_solver_opts* o);
 
 /* Operator::Elastic<T>::define + Operator<Grid::Node>::define (Elastic.cpp:30-55,
- * Operator.cpp:215-258): allocates the multigrid hierarchy and the operator diagonal. */
+ * Operator.cpp:215-258): allocates the multigrid hierarchy and the operator diagonal.
+ * levels: the patches of the AMR hierarchy, level by level.  Entry 0 covers the level-0 domain.
+ * Each finer level refines the one before by 2 (domain_cells doubled); consecutive entries with
+ * the same domain_cells are the patches of one level (an AMReX BoxArray), each nested in one
+ * patch of the level below and separated from the level's other patches: their storage boxes,
+ * the nodal patch grown by 2, may not meet.  Touching boxes whose union is a box are passed as
+ * that one box.  Every other call's amrlev is an index into this list, and solves take one fab
+ * per entry. */
 int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out);
 int ae_op_destroy(ae_op* op);
 /* cudaStream_t passed as void*; NULL selects the operator's own stream, a blocking
