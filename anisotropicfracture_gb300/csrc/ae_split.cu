@@ -182,6 +182,9 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                   const unsigned* __restrict__ gidm_g, const float* __restrict__ tab, int tab_n, float* __restrict__ xo,
                   float omega, int* err) {
     constexpr int NC = NCoef<M>::value;
+    // grain rows in shared memory padded to whole float4s, read four coefficients per load
+    constexpr int NCP = (NC + 3) / 4 * 4;
+    constexpr int TS = TABS ? NCP : NC;  // row stride of the table the kernel reads
     extern __shared__ __align__(128) float smem[];
     const unsigned* gring = reinterpret_cast<const unsigned*>(smem + kOffG);
     int* qn = reinterpret_cast<int*>(smem + kOffQ);
@@ -190,7 +193,11 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     const float* tb = tab;
     if (TABS) {
         float* ts = smem + kOffT;
-        for (int q = threadIdx.x; q < tab_n; q += SNT) ts[q] = __ldg(tab + q);
+        const int rows = tab_n / NC;
+        for (int q = threadIdx.x; q < rows * NCP; q += SNT) {
+            const int g = q / NCP, c = q - g * NCP;
+            ts[q] = c < NC ? __ldg(tab + g * NC + c) : 0.0f;
+        }
         tb = ts;
     }
     const int tx = threadIdx.x % STX, ty = threadIdx.x / STX;
@@ -285,10 +292,21 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                 bb[p][2][1] = bb[p][1][2];
             }
             {
-                float a[NC];
-                const float* a0 = tb + (int)(gw & 0xffffu) * NC;
+                float a[NCP];
+                const float* a0 = tb + (int)(gw & 0xffffu) * TS;
+                if (TABS) {
 #pragma unroll
-                for (int q = 0; q < NC; ++q) a[q] = a0[q];
+                    for (int q = 0; q < NCP; q += 4) {
+                        const float4 v = *reinterpret_cast<const float4*>(a0 + q);
+                        a[q] = v.x;
+                        a[q + 1] = v.y;
+                        a[q + 2] = v.z;
+                        a[q + 3] = v.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) a[q] = a0[q];
+                }
                 div_of<M, float>(a, bb, f);
             }
             queued = !uniform && (gw >> 16) != 0;
@@ -348,8 +366,8 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (mask & (1u << d)) {
-                    const float* cp = tb + gid_n[d][0] * NC;
-                    const float* cm = tb + gid_n[d][1] * NC;
+                    const float* cp = tb + gid_n[d][0] * TS;
+                    const float* cm = tb + gid_n[d][1] * TS;
                     gradC_col_f<M, float>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
                 } else {
                     colv[d][0] = colv[d][1] = colv[d][2] = 0.0f;
@@ -442,6 +460,7 @@ CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUte
     return m;
 }
 
+// tab_n: the table's floats as padded in shared memory
 size_t tile_smem(int tab_n, bool tabs) { return sizeof(float) * (size_t)(kOffT + (tabs ? tab_n : 0)); }
 
 template <int M, bool TABS, int OP>
@@ -477,8 +496,9 @@ void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Bo
         const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32);
         const dim3 grid((unsigned)(T.tiles_x * tiles_y), (unsigned)((nz + T.kz - 1) / T.kz));
         const int tab_n = ngrains * NCoef<Mv>::value;
-        const bool tabs = tab_n * (int)sizeof(float) <= kTabSmemMax;
-        const size_t smem = tile_smem(tab_n, tabs);
+        const int tab_pad = ngrains * ((NCoef<Mv>::value + 3) / 4 * 4);
+        const bool tabs = tab_pad * (int)sizeof(float) <= kTabSmemMax;
+        const size_t smem = tile_smem(tab_pad, tabs);
         if (tabs) {
             tile_smem_attr<Mv, true, OP>(smem);
             k_sweep_tile<Mv, true, OP><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc,

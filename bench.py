@@ -55,6 +55,9 @@ FAPPLY32_BYTES_PER_NODE_GRAINS = 12 + 2 + 12
 # split sweep's tiled kernel over the interior box (x 12, b 12, 1/D 12, id + direction mask 4,
 # out 12 = 52 algorithmic bytes), per node of that box; per node: the one-pass kernel.
 JACOBI32_TRAFFIC_PER_NODE = {True: 52.1, False: 131.1}
+# FP64 operations per node (FMA counted as 2) of the FP64 Fapply on a grain map: ncu counts of
+# DFMA / DADD / DMUL thread instructions at 129^3 nodes
+FAPPLY64_FLOPS_PER_NODE_GRAINS = 215.0
 # FP64 composite iterations the config needs (measured by this benchmark's FP64 solve, which
 # matches the oracle iteration for iteration); used to extrapolate the CPU oracle's per-iteration
 # time to a full solve in the reference arm, which cannot afford a full CPU solve.
@@ -176,6 +179,27 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(n=4096, reps=3):
+    """The FP64 rate the GPU sustains on a cuBLAS DGEMM (torch.matmul of two n x n float64
+    matrices), best of reps, CUDA events: the denominator of the FP64 kernels' FLOP fraction."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 def measured_peaks():
@@ -1225,6 +1249,7 @@ def main():
     _lib.check(lib.ae_profile_kernel(op.handle, 0, 0, 0, 1, 20, C.byref(ms_f32)))
     n0 = int(np.prod(rhs_h[0].shape[1:]))
     peak, peak_kind = measured_peaks()
+    f64_peak = fp64_peak_tflops() if rank == 0 else None
     # achieved = canonical algorithmic bytes (per-node stiffness) / time; the bytes the kernels
     # actually have to move on a grain map (2-byte id per node; the per-grain table stays in
     # L1/L2) are reported beside them
@@ -1285,6 +1310,12 @@ def main():
                      "canonical_gbs": jac_gbs, "canonical_frac": jac_gbs / peak,
                      "canonical": "the same sweep's bytes with a per-node 21-coefficient stiffness (132 B/node)"},
         "fapply": {"fp64_gbs": fapply64_gbs, "fp64_ms": ms_f64.value, "fp32_gbs": fapply32_gbs,
+                   "fp64_tflops": (FAPPLY64_FLOPS_PER_NODE_GRAINS * n0 / (ms_f64.value * 1e-3) / 1e12
+                                   if grains else None),
+                   "fp64_flops_per_node": FAPPLY64_FLOPS_PER_NODE_GRAINS if grains else None,
+                   "fp64_peak_tflops_dgemm": f64_peak,
+                   "fp64_frac_of_dgemm": (FAPPLY64_FLOPS_PER_NODE_GRAINS * n0 / (ms_f64.value * 1e-3) / 1e12 / f64_peak
+                                          if grains and f64_peak else None),
                    "fp32_ms": ms_f32.value, "bytes_per_node_fp64": FAPPLY64_BYTES_PER_NODE,
                    "bytes_per_node_fp32": FAPPLY32_BYTES_PER_NODE,
                    "actual_bytes_per_node_fp64": a_f64, "actual_bytes_per_node_fp32": a_f32},
