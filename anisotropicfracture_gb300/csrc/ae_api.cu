@@ -143,6 +143,7 @@ struct ae_op_s {
     bool prepared32 = false;
     bool tiled32 = false, tiled64 = false;  // z-marching tiled sweeps per precision (opt-in)
     bool split32 = true;                    // split FP32 sweeps on grain-map levels (AE_SPLIT=0: off)
+    bool zero_sweep = true;                 // stencil-free first sweep from a zero correction (AE_ZERO_SWEEP=0: off)
     long long bytes = 0;
     std::vector<void*> allocs;
     void* stage = nullptr;  // device staging for host fabs
@@ -560,14 +561,20 @@ struct Cycle {
     std::vector<MGLevel>& lv;
     cudaStream_t st;
 
-    // one smoother call (Fsmooth): o.sweeps Jacobi sweeps, x ping-pongs through tmp
-    void smooth(int m, R* x, const R* b) {
+    // one smoother call (Fsmooth): o.sweeps Jacobi sweeps, x ping-pongs through tmp.  from_zero:
+    // x is known to be zero (and need not hold it): the first sweep is the stencil-free one.
+    void smooth(int m, R* x, const R* b, bool from_zero = false) {
         MGLevel& L = lv[m];
         LevelPtrs<R> p = ptrs<R>(L);
         R* a = x;
         R* t = p.tmp;
         for (int s = 0; s < o.sweeps; ++s) {
-            sweep_jacobi<R>(op, L.g, p.C, p.invD, p.D, a, b, t, (R)o.omega, st);
+            if (s == 0 && from_zero)
+                launch_jacobi_zero<R>(L.g, cview(level_view(L.g, const_cast<R*>(p.invD))),
+                                      cview(level_view(L.g, const_cast<R*>(p.D))), cview(level_view(L.g, const_cast<R*>(b))),
+                                      level_view(L.g, t), (R)o.omega, st);
+            else
+                sweep_jacobi<R>(op, L.g, p.C, p.invD, p.D, a, b, t, (R)o.omega, st);
             std::swap(a, t);
         }
         if (a != x) launch_copy<R, R>(geo_store(L.g), 3, level_view(L.g, x), cview(level_view(L.g, a)), st);
@@ -619,8 +626,9 @@ struct Cycle {
         const int bot = (int)lv.size() - 1;
         for (int m = top; m < bot; ++m) {
             LevelPtrs<R> p = ptrs<R>(lv[m]);
-            zero(m, p.cor);
-            for (int i = 0; i < o.nu1; ++i) smooth(m, p.cor, p.res);
+            const bool z = op->zero_sweep && o.nu1 > 0 && o.sweeps > 0;
+            if (!z) zero(m, p.cor);
+            for (int i = 0; i < o.nu1; ++i) smooth(m, p.cor, p.res, z && i == 0);
             res_of_cor(m);
             restrict_res(m, p.rescor);
         }
@@ -692,9 +700,10 @@ struct AmrIter {
     }
     void add_cor(int a) { launch_axpy<R, R>(store_dom(a), 3, V(a, sol[a]), 1.0, CV(a, P(a).cor), st); }
     void mini_cycle(int a) {
-        launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
+        const bool z = op->zero_sweep && o.nu1 + o.nu2 > 0 && o.sweeps > 0;
+        if (!z) launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
         Cycle<R> cy{op, o, op->amr[a].mg, st};
-        for (int i = 0; i < o.nu1 + o.nu2; ++i) cy.smooth(0, P(a).cor, P(a).res);
+        for (int i = 0; i < o.nu1 + o.nu2; ++i) cy.smooth(0, P(a).cor, P(a).res, z && i == 0);
     }
     void interp_cor(int a) {
         launch_fill<R>(geo_store(G(a)), 3, V(a, P(a).cor), R(0), st);
@@ -1053,6 +1062,7 @@ int ae_op_create(const ae_level_desc* levels, int nlev, int model, ae_op** out) 
         if (const char* e = std::getenv("AE_TILED32")) op->tiled32 = std::atoi(e) != 0;
         if (const char* e = std::getenv("AE_TILED64")) op->tiled64 = std::atoi(e) != 0;
         if (const char* e = std::getenv("AE_SPLIT")) op->split32 = std::atoi(e) != 0;
+        if (const char* e = std::getenv("AE_ZERO_SWEEP")) op->zero_sweep = std::atoi(e) != 0;
         if (model == AE_MODEL_MAJOR) op->tiled32 = op->tiled64 = false;  // per-node kernels only
         tiled_init<float>();
         tiled_init<double>();

@@ -173,6 +173,23 @@ __global__ void __launch_bounds__(kBlock, sweep_min_blocks<R, GR>()) k_residual(
 
 // ------------------------------------------------------------------ damped Jacobi sweep
 // src/Operator/Operator.cpp:109-157 with the per-node Fapply fused in: one node (i, j, k).
+// The damped-Jacobi update of one component: x_new from x, (A x), b, D and 1/D.
+__device__ __forceinline__ double jacobi_update_impl(double xv, double ax, double b, double d, double invd,
+                                                     double omega) {
+    // the reference's update, (1-w) x + w (b - (Ax - D x)) / D (Operator.cpp:154)
+    const double dx = xv * d;
+    const double rx = ax - dx;
+    return (1.0 - omega) * xv + omega * (b - rx) * invd;
+}
+__device__ __forceinline__ float jacobi_update_impl(float xv, float ax, float b, float, float invd, float omega) {
+    // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D
+    return xv + omega * (b - ax) * invd;
+}
+template <class R>
+__device__ __forceinline__ R jacobi_update(R xv, R ax, R b, R d, R invd, R omega) {
+    return jacobi_update_impl(xv, ax, b, d, invd, omega);
+}
+
 template <int M, class R, bool GR, bool SAME>
 __device__ __forceinline__ void jacobi_node(const OpParams& P, const SCoef<R>& K, const View<const R>& C,
                                             const Grains<R>& G, const View<const R>& invD, const View<const R>& D,
@@ -200,18 +217,36 @@ __device__ __forceinline__ void jacobi_node(const OpParams& P, const SCoef<R>& K
     const long long od = SAME ? ox : invD.at(i, j, k), ob = SAME ? ox : b.at(i, j, k);
     const long long dsc = SAME ? xsc : D.sc, isc = SAME ? xsc : invD.sc, bsc = SAME ? xsc : b.sc;
 #pragma unroll
-    for (int n = 0; n < 3; ++n) {
-        const R xv = xi.p[ox + n * xsc];
-        if (sizeof(R) == 8) {
-            // the reference's update, (1-w) x + w (b - (Ax - D x)) / D (Operator.cpp:154)
-            const R dx = xv * D.p[od + n * dsc];
-            const R rx = v[n] - dx;
-            xo.p[oo + n * osc] = (R(1) - omega) * xv + omega * (b.p[ob + n * bsc] - rx) * invD.p[od + n * isc];
-        } else {
-            // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D
-            xo.p[oo + n * osc] = xv + omega * (b.p[ob + n * bsc] - v[n]) * invD.p[od + n * isc];
-        }
+    for (int n = 0; n < 3; ++n)
+        xo.p[oo + n * osc] = jacobi_update<R>(xi.p[ox + n * xsc], v[n], b.p[ob + n * bsc],
+                                              sizeof(R) == 8 ? D.p[od + n * dsc] : R(0), invD.p[od + n * isc], omega);
+}
+
+// The first sweep of a smoother call whose correction starts at zero (the pre-smoothing of a
+// V-cycle level, a patch's mini-cycle): A 0 = 0 on every row, interior and boundary, so the
+// sweep needs no stencil.  Every node gets what jacobi_node gives it for x = 0 and A x = 0,
+// through the same update with the zeros passed in at run time (zero == 0), so the arithmetic
+// and its rounding are the full sweep's.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_jacobi_zero(Geo g, Reg reg, View<const R> invD, View<const R> D,
+                                                        View<const R> b, View<R> xo, R omega, R zero) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= reg.n) return;
+    int i, j, k;
+    reg_ijk(reg, t, i, j, k);
+    const long long oo = xo.at(i, j, k);
+    const bool ring = g.ng >= 2 && (i == g.vlo[0] - 2 || i == g.vhi[0] + 2 || j == g.vlo[1] - 2 || j == g.vhi[1] + 2 ||
+                                    k == g.vlo[2] - 2 || k == g.vhi[2] + 2);
+    if (!in_box(g.dlo, g.dhi, i, j, k) || ring) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) xo.p[oo + n * xo.sc] = zero;
+        return;
     }
+    const long long od = invD.at(i, j, k), ob = b.at(i, j, k);
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+        xo.p[oo + n * xo.sc] = jacobi_update<R>(zero, zero, b.p[ob + n * b.sc], sizeof(R) == 8 ? D.p[od + n * D.sc] : R(0),
+                                                invD.p[od + n * invD.sc], omega);
 }
 
 template <int M, class R, bool GR, bool SAME>
@@ -405,17 +440,10 @@ __global__ void __launch_bounds__(TX* TY, 2) k_tiled(OpParams P, SCoef<R> K, Box
                 } else {
                     const long long ob = b.at(i, j, k), od = invD.at(i, j, k);
 #pragma unroll
-                    for (int n = 0; n < 3; ++n) {
-                        const R xv = Uc[n * HP + idx];
-                        if (sizeof(R) == 8) {
-                            const R rx = f[n] - xv * D.p[od + n * D.sc];
-                            out.p[oo + n * out.sc] =
-                                (R(1) - omega) * xv + omega * (b.p[ob + n * b.sc] - rx) * invD.p[od + n * invD.sc];
-                        } else {
-                            out.p[oo + n * out.sc] =
-                                xv + omega * (b.p[ob + n * b.sc] - f[n]) * invD.p[od + n * invD.sc];
-                        }
-                    }
+                    for (int n = 0; n < 3; ++n)
+                        out.p[oo + n * out.sc] = jacobi_update<R>(Uc[n * HP + idx], f[n], b.p[ob + n * b.sc],
+                                                                  sizeof(R) == 8 ? D.p[od + n * D.sc] : R(0),
+                                                                  invD.p[od + n * invD.sc], omega);
                 }
             }
         }

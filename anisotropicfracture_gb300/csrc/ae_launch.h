@@ -151,6 +151,11 @@ template <class Ro, class Ri>
 void launch_axpy(const Box3& region, int ncomp, View<Ro> dst, double alpha, View<const Ri> src, cudaStream_t st);
 template <class R>
 void launch_fill(const Box3& region, int ncomp, View<R> dst, R value, cudaStream_t st);
+// The first damped-Jacobi sweep from x = 0 over the level's storage box: every node as the full
+// sweep leaves it for x = 0 (x_new = w b / D where the sweep updates, 0 elsewhere), no stencil.
+template <class R>
+void launch_jacobi_zero(const Geo& g, View<const R> invD, View<const R> D, View<const R> b, View<R> xo, R omega,
+                        cudaStream_t st);
 // max |v| over region into *norm (bit pattern)
 template <class R>
 void launch_norminf(const Box3& region, int ncomp, View<const R> v, unsigned long long* norm, cudaStream_t st);

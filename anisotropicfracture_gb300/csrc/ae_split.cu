@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
         if (act && !queued) {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                if (OP == SPLIT_JACOBI) xo[o + n * sc] = xv[n] + omega * (bv[n * SVP] - f[n]) * dv[n * SVP];
+                if (OP == SPLIT_JACOBI) xo[o + n * sc] = jacobi_update<float>(xv[n], f[n], bv[n * SVP], 0.0f, dv[n * SVP], omega);
                 else xo[o + n * sc] = bv[n * SVP] - f[n];
             }
         }
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             for (int r = 0; r < 3; ++r) {
                 float fr = qf[3 * e + r];
                 fr += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
-                if (OP == SPLIT_JACOBI) xo[qo + r * sc] = qc[r * SXP] + omega * (qb[r * SVP] - fr) * qd[r * SVP];
+                if (OP == SPLIT_JACOBI) xo[qo + r * sc] = jacobi_update<float>(qc[r * SXP], fr, qb[r * SVP], 0.0f, qd[r * SVP], omega);
                 else xo[qo + r * sc] = qb[r * SVP] - fr;
             }
         }
