@@ -186,12 +186,15 @@ struct ae_op_s {
         P.uniform = uniform;
         return P;
     }
-    // the grain-map level whose FP32 stiffness is C, when its sweeps are split; else nullptr
-    const MGLevel* split_for(const float* C) const {
+    // the grain-map level whose stiffness (FP32 copy or FP64) is C, when its sweeps are split;
+    // else nullptr
+    template <class R>
+    const MGLevel* split_for(const R* C) const {
         if (!split32) return nullptr;
         for (const AmrLevel& A : amr) {
             const MGLevel& L = A.mg[0];
-            if (L.grains && L.split_built && C == L.C32) return &L;
+            const void* mine = sizeof(R) == 4 ? static_cast<const void*>(L.C32) : static_cast<const void*>(L.C);
+            if (L.grains && L.split_built && static_cast<const void*>(C) == mine) return &L;
         }
         return nullptr;
     }
@@ -408,18 +411,21 @@ void prepare32(ae_op* op) {
         }
     AE_CHECK(cudaStreamSynchronize(op->st));
     assemble_bottom(op);
-    // node lists and id/mask arrays of the split FP32 sweeps on grain-map levels
-    if (op->split32)
-        for (auto& A : op->amr) {
-            MGLevel& L = A.mg[0];
-            if (!L.grains || L.split_built || (L.g.ng != 0 && L.g.ng < 2) || L.ngrains > kSplitMaxGrains ||
-                !split_supported(L.g))
-                continue;
-            split_build(L.g, cview(level_view(L.g, L.gid)), L.split, op->st, op->dnorm + 7);
-            if (const char* e = std::getenv("AE_SPLIT_KZ")) L.split.kz = std::atoi(e);
-            L.split_built = true;
-        }
     op->prepared32 = true;
+}
+
+// node lists and id/mask arrays of the split sweeps (FP32 and FP64) on grain-map levels
+void build_splits(ae_op* op) {
+    if (!op->split32) return;
+    for (auto& A : op->amr) {
+        MGLevel& L = A.mg[0];
+        if (!L.grains || L.split_built || (L.g.ng != 0 && L.g.ng < 2) || L.ngrains > kSplitMaxGrains ||
+            !split_supported(L.g))
+            continue;
+        split_build(L.g, cview(level_view(L.g, L.gid)), L.split, op->st, op->dnorm + 7);
+        if (const char* e = std::getenv("AE_SPLIT_KZ")) L.split.kz = std::atoi(e);
+        L.split_built = true;
+    }
 }
 
 // dflag[2] is set by the split sweep's tiled kernel when a TMA load did not complete within its
@@ -470,6 +476,7 @@ void prepare(ae_op* op) {
     int flag = 0;
     AE_CHECK(cudaMemcpyAsync(&flag, op->dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
     AE_CHECK(cudaStreamSynchronize(st));
+    build_splits(op);
     op->prepared = true;
     if (flag) {
         op->prepared = false;
@@ -493,14 +500,11 @@ void sweep_jacobi(ae_op* op, const Geo& g, const R* C, const R* invD, const R* D
         launch_tiled<R>(1, P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(xi))),
                         cview(level_view(g, const_cast<R*>(b))), cview(level_view(g, const_cast<R*>(invD))),
                         cview(level_view(g, const_cast<R*>(D))), level_view(g, xo), omega, st);
-    else if (const MGLevel* sl = sizeof(R) == 4 ? op->split_for(reinterpret_cast<const float*>(C)) : nullptr)
-        launch_jacobi_split(P, sl->split, cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(C)))),
-                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(invD)))),
-                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(D)))),
-                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(xi)))),
-                            cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(b)))),
-                            level_view(g, reinterpret_cast<float*>(xo)), (float)omega, st,
-                            op->grains_for<float>(reinterpret_cast<const float*>(C)), sl->ngrains, op->dflag + 2);
+    else if (const MGLevel* sl = op->split_for<R>(C))
+        launch_jacobi_split<R>(P, sl->split, cview(level_view(g, const_cast<R*>(C))),
+                               cview(level_view(g, const_cast<R*>(invD))), cview(level_view(g, const_cast<R*>(D))),
+                               cview(level_view(g, const_cast<R*>(xi))), cview(level_view(g, const_cast<R*>(b))),
+                               level_view(g, xo), omega, st, op->grains_for<R>(C), sl->ngrains, op->dflag + 2);
     else
         launch_jacobi<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(invD))),
                          cview(level_view(g, const_cast<R*>(D))), cview(level_view(g, const_cast<R*>(xi))),
@@ -515,12 +519,10 @@ void sweep_residual(ae_op* op, const Geo& g, const R* C, const R* x, const R* b,
         launch_tiled<R>(2, P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                         cview(level_view(g, const_cast<R*>(b))), cview(level_view(g, const_cast<R*>(b))),
                         cview(level_view(g, const_cast<R*>(b))), level_view(g, r), R(0), st);
-    else if (const MGLevel* sl = sizeof(R) == 4 ? op->split_for(reinterpret_cast<const float*>(C)) : nullptr)
-        launch_residual_split(P, sl->split, cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(C)))),
-                              cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(x)))),
-                              cview(level_view(g, const_cast<float*>(reinterpret_cast<const float*>(b)))),
-                              level_view(g, reinterpret_cast<float*>(r)), st,
-                              op->grains_for<float>(reinterpret_cast<const float*>(C)), sl->ngrains, op->dflag + 2);
+    else if (const MGLevel* sl = op->split_for<R>(C))
+        launch_residual_split<R>(P, sl->split, cview(level_view(g, const_cast<R*>(C))),
+                                 cview(level_view(g, const_cast<R*>(x))), cview(level_view(g, const_cast<R*>(b))),
+                                 level_view(g, r), st, op->grains_for<R>(C), sl->ngrains, op->dflag + 2);
     else
         launch_residual<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                            cview(level_view(g, const_cast<R*>(b))), level_view(g, r), nullptr, nullptr, st,

@@ -547,7 +547,7 @@ struct BottomOps {
     View<const double> Cv;
     const double* D;
     const double* invD;
-    long long sy, sz, nn;
+    int sy, sz, nn;  // the coarsest level is small: 32-bit index arithmetic
     int nx, ny, nz;
     __device__ BottomOps(const BottomArgs& aa, const double* C, const double* D_, const double* invD_)
         : a(aa), D(D_), invD(invD_) {
@@ -557,7 +557,7 @@ struct BottomOps {
         ny = g.vhi[1] - g.vlo[1] + 1;
         nz = g.vhi[2] - g.vlo[2] + 1;
         sy = nx;
-        sz = (long long)nx * ny;
+        sz = nx * ny;
         nn = sz * nz;
         Cv.p = C;
         Cv.lo[0] = g.vlo[0]; Cv.lo[1] = g.vlo[1]; Cv.lo[2] = g.vlo[2];
@@ -566,8 +566,8 @@ struct BottomOps {
     // out = A x over every node
     __device__ void apply(const double* x, double* out, BlkRed&) const {
         const Geo& g = a.P.g;
-        for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
-            const int k = (int)(t / sz), rem = (int)(t - (long long)k * sz);
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            const int k = t / sz, rem = t - k * sz;
             const int j = rem / nx, i = rem - j * nx;
             double v[3];
             apply_node<M, double, !SMEM>(g, K, a.P.bc, a.P.uniform, Cv.p, nn, t, sy, sz, x, nn, t, sy, sz,
@@ -580,24 +580,24 @@ struct BottomOps {
     }
     __device__ void residual(const double* x, const double* b, double* r, BlkRed& sh) const {
         apply(x, r, sh);
-        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) r[t] = b[t] - r[t];
+        for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) r[t] = b[t] - r[t];
         __syncthreads();
     }
     __device__ double dot(const double* x, const double* y, BlkRed& sh) const {
         double s = 0.0;
-        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) s += x[t] * y[t];
+        for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) s += x[t] * y[t];
         return blk_sum(s, sh);
     }
     __device__ double ninf(const double* x, BlkRed& sh) const {
         double s = 0.0;
-        for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) s = fmax(s, fabs(x[t]));
+        for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) s = fmax(s, fabs(x[t]));
         return blk_max(s, sh);
     }
     // one Fsmooth call: a.sweeps damped-Jacobi sweeps (ng = 0: every node is updated)
     __device__ void smooth(double* x, const double* b, double* tmp, BlkRed& sh) const {
         for (int s = 0; s < a.sweeps; ++s) {
             apply(x, tmp, sh);
-            for (long long t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
+            for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
                 const double xv = x[t];
                 const double rx = tmp[t] - xv * D[t];
                 x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * invD[t];
@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
     __shared__ BlkRed sh;
     extern __shared__ double smem[];
     constexpr int NC = NCoef<M>::value;
-    const long long N = 3 * a.nn;
+    const int N = (int)(3 * a.nn);
     const double* Cp = a.C;
     const double* Dp = a.D;
     const double* invDp = a.invD;
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
         double* sb = sI + N;
         double* sx = sb + N;
         for (long long t = threadIdx.x; t < NC * a.nn; t += blockDim.x) sC[t] = a.C[t];
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
             sD[t] = a.D[t];
             sI[t] = a.invD[t];
             sb[t] = a.b[t];
@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom(BottomArgs a) {
     const int ret = krylov_bottom(ops, kp, N, x, b, work, sh);
     if (ret != 0 && ret != 9 && threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
     if (SMEM) {
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
+        for (int t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
     }
 }
 
@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(128) k_bottom_assemble(BottomArgs a, double* A
     const long long nn = a.nn, N = 3 * nn;
     const long long j = blockIdx.x;
     double* e = E + j * N;
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) e[t] = (t == j) ? 1.0 : 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) e[t] = (t == j) ? 1.0 : 0.0;
     __syncthreads();
     const Geo& g = a.P.g;
     const int nx = g.vhi[0] - g.vlo[0] + 1, ny = g.vhi[1] - g.vlo[1] + 1;
@@ -737,9 +737,9 @@ struct CsrOps {
     const int* rowptr;
     const int* col;
     const double* val;
-    long long N;
+    int N;
     __device__ void apply(const double* x, double* out, BlkRed&) const {
-        for (long long r = threadIdx.x; r < N; r += blockDim.x) {
+        for (int r = threadIdx.x; r < N; r += blockDim.x) {
             double s = 0.0;
             for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) s += val[q] * x[col[q]];
             out[r] = s;
@@ -748,24 +748,24 @@ struct CsrOps {
     }
     __device__ void residual(const double* x, const double* b, double* r, BlkRed& sh) const {
         apply(x, r, sh);
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) r[t] = b[t] - r[t];
+        for (int t = threadIdx.x; t < N; t += blockDim.x) r[t] = b[t] - r[t];
         __syncthreads();
     }
     __device__ double dot(const double* x, const double* y, BlkRed& sh) const {
         double s = 0.0;
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) s += x[t] * y[t];
+        for (int t = threadIdx.x; t < N; t += blockDim.x) s += x[t] * y[t];
         return blk_sum(s, sh);
     }
     __device__ double ninf(const double* x, BlkRed& sh) const {
         double s = 0.0;
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) s = fmax(s, fabs(x[t]));
+        for (int t = threadIdx.x; t < N; t += blockDim.x) s = fmax(s, fabs(x[t]));
         return blk_max(s, sh);
     }
     // one Fsmooth call with the level's FP64 diagonal (the same update as the stencil form)
     __device__ void smooth(double* x, const double* b, double* tmp, BlkRed& sh) const {
         for (int s = 0; s < a.sweeps; ++s) {
             apply(x, tmp, sh);
-            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            for (int t = threadIdx.x; t < N; t += blockDim.x) {
                 const double xv = x[t];
                 const double rx = tmp[t] - xv * a.D[t];
                 x[t] = (1.0 - a.omega) * xv + a.omega * (b[t] - rx) * a.invD[t];
@@ -780,7 +780,7 @@ template <bool SMEM>
 __global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, BottomCsr m) {
     __shared__ BlkRed sh;
     extern __shared__ double smem[];
-    const long long N = 3 * a.nn;
+    const int N = (int)(3 * a.nn);
     double* x = a.x;
     const double* b = a.b;
     double* work = a.work;
@@ -796,7 +796,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, Bot
         int* scol = srow + N + 1;
         for (long long t = threadIdx.x; t < m.nnz; t += blockDim.x) { sval[t] = m.val[t]; scol[t] = m.col[t]; }
         for (long long t = threadIdx.x; t <= N; t += blockDim.x) srow[t] = m.rowptr[t];
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) { sb[t] = a.b[t]; sx[t] = a.x[t]; }
+        for (int t = threadIdx.x; t < N; t += blockDim.x) { sb[t] = a.b[t]; sx[t] = a.x[t]; }
         __syncthreads();
         rowptr = srow; col = scol; val = sval; b = sb; x = sx; work = sw;
     }
@@ -805,7 +805,7 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, Bot
     const int ret = krylov_bottom(ops, kp, N, x, b, work, sh);
     if (ret != 0 && ret != 9 && threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
     if (SMEM) {
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
+        for (int t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
     }
 }
 
@@ -815,7 +815,7 @@ size_t bottom_csr_smem_bytes(long long N, long long nnz) {
 
 // one thread per row, rounded up to whole warps
 void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st) {
-    const long long N = 3 * a.nn;
+    const int N = (int)(3 * a.nn);
     const int threads = (int)std::min<long long>(kBottomThreads, (N + 31) / 32 * 32);
     const size_t bytes = bottom_csr_smem_bytes(N, m.nnz);
     if (bytes <= kBottomSmemBytes) k_bottom_csr<true><<<1, threads, bytes, st>>>(a, m);

@@ -63,7 +63,7 @@ struct KrylovParams {
 // x: the correction (in: initial guess, out: solution); work: 8 vectors of N doubles.
 // Returns the MLCGSolver status (0 converged; nonzero failed, then x = 0 + nuf smooths).
 template <class Ops>
-__device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N, double* x, const double* b,
+__device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, int N, double* x, const double* b,
                              double* work, BlkRed& sh) {
     double* r = work;
     double* p = r + N;
@@ -74,10 +74,10 @@ __device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N
     double* sorig = tt + N;
     double* tmp = sorig + N;
     const double eps_rel = kp.reltol, eps_abs = -1.0;
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) sorig[t] = x[t];
+    for (int t = threadIdx.x; t < N; t += blockDim.x) sorig[t] = x[t];
     __syncthreads();
     ops.residual(x, b, r, sh);
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
     __syncthreads();
     double rnorm = ops.ninf(r, sh);
     const double rnorm0 = rnorm;
@@ -89,13 +89,13 @@ __device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N
                 const double rho = ops.dot(r, r, sh);  // z = r (no preconditioner)
                 if (rho == 0.0) { ret = 1; break; }
                 const double beta = iter == 1 ? 0.0 : rho / rho_1;
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = iter == 1 ? r[t] : r[t] + beta * p[t];
+                for (int t = threadIdx.x; t < N; t += blockDim.x) p[t] = iter == 1 ? r[t] : r[t] + beta * p[t];
                 __syncthreads();
                 ops.apply(p, q, sh);
                 const double pw = ops.dot(p, q, sh);
                 if (pw == 0.0) { ret = 1; break; }
                 const double alpha = rho / pw;
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * q[t]; }
+                for (int t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * q[t]; }
                 __syncthreads();
                 rnorm = ops.ninf(r, sh);
                 if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
@@ -103,23 +103,23 @@ __device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N
             }
         } else {
             double rho_1 = 0.0, alpha = 0.0, omega = 0.0;
-            for (long long t = threadIdx.x; t < N; t += blockDim.x) { rh[t] = r[t]; p[t] = 0.0; v[t] = 0.0; }
+            for (int t = threadIdx.x; t < N; t += blockDim.x) { rh[t] = r[t]; p[t] = 0.0; v[t] = 0.0; }
             __syncthreads();
             for (int iter = 1; iter <= kp.maxiter; ++iter) {
                 const double rho = ops.dot(rh, r, sh);
                 if (rho == 0.0) { ret = 1; break; }
                 if (iter == 1) {
-                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t];
+                    for (int t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t];
                 } else {
                     const double beta = (rho / rho_1) * (alpha / omega);
-                    for (long long t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t] + beta * (p[t] - omega * v[t]);
+                    for (int t = threadIdx.x; t < N; t += blockDim.x) p[t] = r[t] + beta * (p[t] - omega * v[t]);
                 }
                 __syncthreads();
                 ops.apply(p, v, sh);
                 const double rhTv = ops.dot(rh, v, sh);
                 if (rhTv != 0.0) alpha = rho / rhTv;
                 else { ret = 2; break; }
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * v[t]; }
+                for (int t = threadIdx.x; t < N; t += blockDim.x) { x[t] += alpha * p[t]; r[t] += -alpha * v[t]; }
                 __syncthreads();
                 rnorm = ops.ninf(r, sh);
                 if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
@@ -127,7 +127,7 @@ __device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N
                 const double t_t = ops.dot(tt, tt, sh), t_r = ops.dot(tt, r, sh);
                 if (t_t != 0.0) omega = t_r / t_t;
                 else { ret = 3; break; }
-                for (long long t = threadIdx.x; t < N; t += blockDim.x) { x[t] += omega * r[t]; r[t] += -omega * tt[t]; }
+                for (int t = threadIdx.x; t < N; t += blockDim.x) { x[t] += omega * r[t]; r[t] += -omega * tt[t]; }
                 __syncthreads();
                 rnorm = ops.ninf(r, sh);
                 if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
@@ -138,11 +138,11 @@ __device__ int krylov_bottom(const Ops& ops, const KrylovParams& kp, long long N
         if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
     }
     const bool keep = (ret == 0 || ret == 8) && rnorm < rnorm0;
-    for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = keep ? x[t] + sorig[t] : sorig[t];
+    for (int t = threadIdx.x; t < N; t += blockDim.x) x[t] = keep ? x[t] + sorig[t] : sorig[t];
     __syncthreads();
     // MLMG: on failure the correction is zeroed and nuf smoother calls follow
     if (ret != 0 && ret != 9) {
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) x[t] = 0.0;
         __syncthreads();
         for (int s = 0; s < kp.nuf; ++s) ops.smooth(x, b, tmp, sh);
     }

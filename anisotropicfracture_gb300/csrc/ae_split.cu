@@ -40,30 +40,43 @@ namespace ae {
 namespace {
 
 constexpr int STX = 32, STY = 8, SNT = STX * STY;
-constexpr int SBW = 40;                    // box width: 32 nodes + halo + alignment shift, 160 B
+constexpr int SBW = 40;                    // box width: 32 nodes + halo + alignment shift
 constexpr int SXR = STY + 2;               // x tile rows (one-node halo in j)
-constexpr int SXP = SBW * SXR;             // floats per x component plane tile
-constexpr int SXS = 3 * SXP + 16;          // floats per x ring slot (a multiple of 128 bytes)
-constexpr int SVP = SBW * STY;             // floats per b / 1/D component tile (no halo)
-constexpr int SVS = 3 * SVP;               // floats per b / 1/D ring slot
+constexpr int SXP = SBW * SXR;             // elements per x component plane tile
+constexpr int SVP = SBW * STY;             // elements per b / 1/D / D component tile (no halo)
 constexpr int SXRING = 4, SVRING = 2;      // x planes k-1, k, k+1 + the one in flight; b, 1/D, ids
-constexpr unsigned kXBytes = 3 * SXP * 4, kVBytes = SVS * 4, kGBytes = SVP * 4;
 constexpr int kWaitLimit = 1 << 20;        // try_wait polls before a wait is declared failed
 #ifndef AE_SPLIT_MIN_BLOCKS
 #define AE_SPLIT_MIN_BLOCKS 4
 #endif
 
-// shared memory of the tiled kernel, in floats: x ring, b ring, 1/D ring, id ring (every TMA
-// destination on a 128-byte boundary), two mbarriers, the grain table
-constexpr int kOffB = SXRING * SXS;
-constexpr int kOffD = kOffB + SVRING * SVS;
-constexpr int kOffG = kOffD + SVRING * SVS;
-constexpr int kOffBar = kOffG + SVRING * SVP;
-// queue of the plane's nodes with a non-zero grad C column: count, thread index, main-term f
-constexpr int kOffQ = kOffBar + 4;
-constexpr int kOffT = kOffQ + 4 + SNT + 3 * SNT;
-static_assert((SXS * 4) % 128 == 0 && (SVS * 4) % 128 == 0 && (SVP * 4) % 128 == 0, "TMA slot alignment");
-static_assert((kOffB * 4) % 128 == 0 && (kOffD * 4) % 128 == 0 && (kOffG * 4) % 128 == 0, "TMA ring alignment");
+__host__ __device__ constexpr int up128(int b) { return (b + 127) / 128 * 128; }
+__host__ __device__ constexpr int up16(int b) { return (b + 15) / 16 * 16; }
+
+// Shared memory of the tiled kernel, in bytes, for elements R: the x ring, the b, 1/D and (FP64
+// Jacobi: the reference's update reads D) D rings, the id ring -- every TMA destination on a
+// 128-byte boundary -- two mbarriers, the queue of the plane's nodes with a non-zero grad C
+// column (count, thread index, main-term f) and the grain table.
+template <class R>
+struct TL {
+    static constexpr int E = (int)sizeof(R);
+    static constexpr int XS = up128(3 * SXP * E);  // bytes per x ring slot
+    static constexpr int VS = 3 * SVP * E;         // bytes per b / 1/D / D ring slot
+    static constexpr int GS = SVP * 4;             // bytes per id ring slot
+    static constexpr int oB = SXRING * XS;
+    static constexpr int oI = oB + SVRING * VS;
+    static constexpr int oD = oI + SVRING * VS;
+    static constexpr int oG = oD + (E == 8 ? SVRING * VS : 0);
+    static constexpr int oBar = oG + SVRING * GS;
+    static constexpr int oQ = oBar + 16;
+    static constexpr int oQt = oQ + 16;
+    static constexpr int oQf = up16(oQt + 4 * SNT);
+    static constexpr int oT = up16(oQf + 3 * SNT * E);
+    static constexpr unsigned kX = 3 * SXP * E, kV = 3 * SVP * E, kG = SVP * 4;
+    static_assert(VS % 128 == 0 && GS % 128 == 0 && oB % 128 == 0 && oI % 128 == 0 && oD % 128 == 0 &&
+                      oG % 128 == 0,
+                  "TMA slot alignment");
+};
 constexpr int kTabSmemMax = 24 * 1024;  // bytes of grain table kept in shared memory
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -167,36 +180,39 @@ struct TileGeo {
     int sh;        // column shift of the tile's first halo column inside the box
 };
 
-// One sweep over the interior box I of a grain-map level (FP32), A the interior row of
-// Elastic<T>::Fapply: OP = SPLIT_JACOBI, the damped-Jacobi update out = x + w (b - A x) / D
-// (Operator.cpp:109-157 as the FP32 cycle writes it); OP = SPLIT_RESIDUAL, out = b - A x (out may
-// alias b: each node reads its own b before writing).  gidm: grain id (low 16 bits) and the
-// directions with a non-zero grad C column (bits 16-18).  TABS: grain table in shared memory
-// (tab_n floats) or read through L1.  err: set when a TMA load did not complete.
+// One sweep over the interior box I of a grain-map level, A the interior row of
+// Elastic<T>::Fapply: OP = SPLIT_JACOBI, the damped-Jacobi update (jacobi_update: the reference's
+// form in FP64, x + w (b - A x) / D in the FP32 cycle; Operator.cpp:109-157); OP = SPLIT_RESIDUAL,
+// out = b - A x (out may alias b: every node reads only its own b).  The grain table is staged
+// in shared memory (TABS, rows padded to 16 bytes) or read through L1.  err: set when a TMA load
+// did not complete.
 enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1 };
-template <int M, bool TABS, int OP>
-__global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
+template <int M, class R, bool TABS, int OP>
+__global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     k_sweep_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
-                  const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_g, SCoef<float> K,
-                  TileGeo T, int uniform, long long sy, long long sz, long long sc,
-                  const unsigned* __restrict__ gidm_g, const float* __restrict__ tab, int tab_n, float* __restrict__ xo,
-                  float omega, int* err) {
+                 const __grid_constant__ CUtensorMap tm_i, const __grid_constant__ CUtensorMap tm_d,
+                 const __grid_constant__ CUtensorMap tm_g, SCoef<R> K, TileGeo T, int uniform, long long sy,
+                 long long sz, long long sc, const unsigned* __restrict__ gidm_g, const R* __restrict__ tab, int tab_n,
+                 R* __restrict__ xo, R omega, int* err) {
+    using L = TL<R>;
     constexpr int NC = NCoef<M>::value;
-    // grain rows in shared memory padded to whole float4s, read four coefficients per load
+    // grain rows in shared memory padded to whole 16-byte vectors (four coefficients)
     constexpr int NCP = (NC + 3) / 4 * 4;
     constexpr int TS = TABS ? NCP : NC;  // row stride of the table the kernel reads
-    extern __shared__ __align__(128) float smem[];
-    const unsigned* gring = reinterpret_cast<const unsigned*>(smem + kOffG);
-    int* qn = reinterpret_cast<int*>(smem + kOffQ);
-    int* qtid = qn + 4;
-    float* qf = smem + kOffQ + 4 + SNT;
-    const float* tb = tab;
+    constexpr bool D64 = sizeof(R) == 8 && OP == SPLIT_JACOBI;
+    extern __shared__ __align__(128) unsigned char smem[];
+    auto xslot = [&](int k) { return reinterpret_cast<const R*>(smem + (k & 3) * L::XS); };
+    const unsigned* gring = reinterpret_cast<const unsigned*>(smem + L::oG);
+    int* qn = reinterpret_cast<int*>(smem + L::oQ);
+    int* qtid = reinterpret_cast<int*>(smem + L::oQt);
+    R* qf = reinterpret_cast<R*>(smem + L::oQf);
+    const R* tb = tab;
     if (TABS) {
-        float* ts = smem + kOffT;
+        R* ts = reinterpret_cast<R*>(smem + L::oT);
         const int rows = tab_n / NC;
         for (int q = threadIdx.x; q < rows * NCP; q += SNT) {
             const int g = q / NCP, c = q - g * NCP;
-            ts[q] = c < NC ? __ldg(tab + g * NC + c) : 0.0f;
+            ts[q] = c < NC ? __ldg(tab + g * NC + c) : R(0);
         }
         tb = ts;
     }
@@ -210,7 +226,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     const int xa = i0 - 1 - T.slo[0] - T.sh;
     const int yx = j0 - 1 - T.slo[1], yv = j0 - T.slo[1];
     const unsigned sb = smem_u32(smem);
-    const unsigned bar0 = sb + 4u * kOffBar;
+    const unsigned bar0 = sb + (unsigned)L::oBar;
     const bool leader = threadIdx.x == 0;
     if (leader) {
         *qn = 0;
@@ -220,18 +236,19 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     }
     __syncthreads();
     auto load_x = [&](int k, unsigned bar) {
-        tma_load4(sb + 4u * (unsigned)((k & 3) * SXS), &tm_x, xa, yx, k - T.slo[2], 0, bar);
+        tma_load4(sb + (unsigned)((k & 3) * L::XS), &tm_x, xa, yx, k - T.slo[2], 0, bar);
     };
     auto load_v = [&](int k, unsigned bar) {
         const unsigned s = (unsigned)(k & 1);
-        tma_load4(sb + 4u * (kOffB + s * SVS), &tm_b, xa, yv, k - T.slo[2], 0, bar);
-        if (OP == SPLIT_JACOBI) tma_load4(sb + 4u * (kOffD + s * SVS), &tm_d, xa, yv, k - T.slo[2], 0, bar);
-        tma_load4(sb + 4u * (kOffG + s * SVP), &tm_g, xa, yv, k - T.slo[2], 0, bar);
+        tma_load4(sb + (unsigned)L::oB + s * L::VS, &tm_b, xa, yv, k - T.slo[2], 0, bar);
+        if (OP == SPLIT_JACOBI) tma_load4(sb + (unsigned)L::oI + s * L::VS, &tm_i, xa, yv, k - T.slo[2], 0, bar);
+        if (D64) tma_load4(sb + (unsigned)L::oD + s * L::VS, &tm_d, xa, yv, k - T.slo[2], 0, bar);
+        tma_load4(sb + (unsigned)L::oG + s * L::GS, &tm_g, xa, yv, k - T.slo[2], 0, bar);
     };
-    constexpr unsigned kVTile = (OP == SPLIT_JACOBI ? 2 : 1) * kVBytes + kGBytes;
-    // stage 0: planes k0-1, k0, k0+1 of x and the b, 1/D, id tiles of plane k0
+    constexpr unsigned kVTile = (OP == SPLIT_JACOBI ? (D64 ? 3 : 2) : 1) * L::kV + L::kG;
+    // stage 0: planes k0-1, k0, k0+1 of x and the b, 1/D (D), id tiles of plane k0
     if (leader) {
-        mbar_expect_tx(bar0, 3 * kXBytes + kVTile);
+        mbar_expect_tx(bar0, 3 * L::kX + kVTile);
         load_x(k0 - 1, bar0);
         load_x(k0, bar0);
         load_x(k0 + 1, bar0);
@@ -252,7 +269,7 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             if (leader) {
                 const unsigned bn = bar0 + 8u * (unsigned)((s + 1) & 1);
                 asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                mbar_expect_tx(bn, kXBytes + kVTile);
+                mbar_expect_tx(bn, L::kX + kVTile);
                 load_x(k + 2, bn);
                 load_v(k + 1, bn);
             }
@@ -263,27 +280,28 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             break;
         }
         const unsigned vs = (unsigned)(k & 1);
-        const float* pm = smem + ((k - 1) & 3) * SXS + cx;
-        const float* pc = smem + (k & 3) * SXS + cx;
-        const float* pp = smem + ((k + 1) & 3) * SXS + cx;
-        const float* bv = smem + kOffB + vs * SVS + cv;
-        const float* dv = smem + kOffD + vs * SVS + cv;
+        const R* pm = xslot(k - 1) + cx;
+        const R* pc = xslot(k) + cx;
+        const R* pp = xslot(k + 1) + cx;
+        const R* bv = reinterpret_cast<const R*>(smem + L::oB + vs * L::VS) + cv;
+        const R* iv = reinterpret_cast<const R*>(smem + L::oI + vs * L::VS) + cv;
+        const R* dv = reinterpret_cast<const R*>(smem + L::oD + vs * L::VS) + cv;
         bool queued = false;
-        float f[3], xv[3];
+        R f[3], xv[3];
         if (act) {
             const unsigned gw = gring[vs * SVP + cv];
-            float bb[3][3][3];
+            R bb[3][3][3];
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
-                const float* um = pm + p * SXP;
-                const float* uc = pc + p * SXP;
-                const float* up = pp + p * SXP;
-                const float c0 = uc[0];
+                const R* um = pm + p * SXP;
+                const R* uc = pc + p * SXP;
+                const R* up = pp + p * SXP;
+                const R c0 = uc[0];
                 xv[p] = c0;
-                const float xm = uc[-1], xp = uc[1], ym = uc[-SBW], yp = uc[SBW], zm = um[0], zp = up[0];
-                bb[p][0][0] = (xp - 2.0f * c0 + xm) * K.i2[0];
-                bb[p][1][1] = (yp - 2.0f * c0 + ym) * K.i2[1];
-                bb[p][2][2] = (zp - 2.0f * c0 + zm) * K.i2[2];
+                const R xm = uc[-1], xp = uc[1], ym = uc[-SBW], yp = uc[SBW], zm = um[0], zp = up[0];
+                bb[p][0][0] = (xp - R(2) * c0 + xm) * K.i2[0];
+                bb[p][1][1] = (yp - R(2) * c0 + ym) * K.i2[1];
+                bb[p][2][2] = (zp - R(2) * c0 + zm) * K.i2[2];
                 bb[p][0][1] = (uc[1 + SBW] + uc[-1 - SBW] - uc[1 - SBW] - uc[-1 + SBW]) * K.m01;
                 bb[p][0][2] = (up[1] + um[-1] - um[1] - up[-1]) * K.m02;
                 bb[p][1][2] = (up[SBW] + um[-SBW] - um[SBW] - up[-SBW]) * K.m12;
@@ -292,22 +310,31 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                 bb[p][2][1] = bb[p][1][2];
             }
             {
-                float a[NCP];
-                const float* a0 = tb + (int)(gw & 0xffffu) * TS;
+                R a[NCP];
+                const R* a0 = tb + (int)(gw & 0xffffu) * TS;
                 if (TABS) {
+                    if (sizeof(R) == 4) {
 #pragma unroll
-                    for (int q = 0; q < NCP; q += 4) {
-                        const float4 v = *reinterpret_cast<const float4*>(a0 + q);
-                        a[q] = v.x;
-                        a[q + 1] = v.y;
-                        a[q + 2] = v.z;
-                        a[q + 3] = v.w;
+                        for (int q = 0; q < NCP; q += 4) {
+                            const float4 v = *reinterpret_cast<const float4*>(a0 + q);
+                            a[q] = (R)v.x;
+                            a[q + 1] = (R)v.y;
+                            a[q + 2] = (R)v.z;
+                            a[q + 3] = (R)v.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < NCP; q += 2) {
+                            const double2 v = *reinterpret_cast<const double2*>(a0 + q);
+                            a[q] = (R)v.x;
+                            a[q + 1] = (R)v.y;
+                        }
                     }
                 } else {
 #pragma unroll
                     for (int q = 0; q < NC; ++q) a[q] = a0[q];
                 }
-                div_of<M, float>(a, bb, f);
+                div_of<M, R>(a, bb, f);
             }
             queued = !uniform && (gw >> 16) != 0;
         }
@@ -332,8 +359,10 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
         if (act && !queued) {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                if (OP == SPLIT_JACOBI) xo[o + n * sc] = jacobi_update<float>(xv[n], f[n], bv[n * SVP], 0.0f, dv[n * SVP], omega);
-                else xo[o + n * sc] = bv[n * SVP] - f[n];
+                if (OP == SPLIT_JACOBI)
+                    xo[o + n * sc] = jacobi_update<R>(xv[n], f[n], bv[n * SVP], D64 ? dv[n * SVP] : R(0), iv[n * SVP], omega);
+                else
+                    xo[o + n * sc] = bv[n * SVP] - f[n];
             }
         }
         __syncthreads();
@@ -344,10 +373,10 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
             const int qx = t % STX, qy = t / STX;
             const int qcx = (qy + 1) * SBW + T.sh + 1 + qx, qcv = qy * SBW + T.sh + 1 + qx;
             const long long qo = o + (long long)(qx - tx) + (long long)(qy - ty) * sy;
-            const float* qm = smem + ((k - 1) & 3) * SXS + qcx;
-            const float* qc = smem + (k & 3) * SXS + qcx;
-            const float* qp = smem + ((k + 1) & 3) * SXS + qcx;
-            float gu[3][3];
+            const R* qm = xslot(k - 1) + qcx;
+            const R* qc = xslot(k) + qcx;
+            const R* qp = xslot(k + 1) + qcx;
+            R gu[3][3];
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 gu[p][0] = (qc[p * SXP + 1] - qc[p * SXP - 1]) * K.h[0];
@@ -362,25 +391,29 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
                 {(int)((qy + 1 < STY ? gv[SBW] : __ldg(gidm_g + qo + sy)) & 0xffffu),
                  (int)((qy > 0 ? gv[-SBW] : __ldg(gidm_g + qo - sy)) & 0xffffu)},
                 {(int)(__ldg(gidm_g + qo + sz) & 0xffffu), (int)(__ldg(gidm_g + qo - sz) & 0xffffu)}};
-            float colv[3][3];
+            R colv[3][3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (mask & (1u << d)) {
-                    const float* cp = tb + gid_n[d][0] * TS;
-                    const float* cm = tb + gid_n[d][1] * TS;
-                    gradC_col_f<M, float>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
+                    const R* cp = tb + gid_n[d][0] * TS;
+                    const R* cm = tb + gid_n[d][1] * TS;
+                    gradC_col_f<M, R>([&](int q) { return cp[q] - cm[q]; }, gu, d, colv[d]);
                 } else {
-                    colv[d][0] = colv[d][1] = colv[d][2] = 0.0f;
+                    colv[d][0] = colv[d][1] = colv[d][2] = R(0);
                 }
             }
-            const float* qb = smem + kOffB + vs * SVS + qcv;
-            const float* qd = smem + kOffD + vs * SVS + qcv;
+            const R* qb = reinterpret_cast<const R*>(smem + L::oB + vs * L::VS) + qcv;
+            const R* qi = reinterpret_cast<const R*>(smem + L::oI + vs * L::VS) + qcv;
+            const R* qd = reinterpret_cast<const R*>(smem + L::oD + vs * L::VS) + qcv;
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
-                float fr = qf[3 * e + r];
+                R fr = qf[3 * e + r];
                 fr += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
-                if (OP == SPLIT_JACOBI) xo[qo + r * sc] = jacobi_update<float>(qc[r * SXP], fr, qb[r * SVP], 0.0f, qd[r * SVP], omega);
-                else xo[qo + r * sc] = qb[r * SVP] - fr;
+                if (OP == SPLIT_JACOBI)
+                    xo[qo + r * sc] = jacobi_update<R>(qc[r * SXP], fr, qb[r * SVP], D64 ? qd[r * SVP] : R(0),
+                                                       qi[r * SVP], omega);
+                else
+                    xo[qo + r * sc] = qb[r * SVP] - fr;
             }
         }
         __syncthreads();
@@ -393,34 +426,34 @@ __global__ void __launch_bounds__(SNT, AE_SPLIT_MIN_BLOCKS)
     }
 }
 
-// 4 resident blocks (64 registers): at 48 the cubic variant spills
-template <int M, bool SAME>
-__global__ void __launch_bounds__(kBlock, 4)
-    k_jacobi_list(OpParams P, SCoef<float> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
-                  View<const float> C, Grains<float> G, View<const float> invD, View<const float> D,
-                  View<const float> xi, View<const float> b, View<float> xo, float omega) {
+// FP32: 4 resident blocks (64 registers): at 48 the cubic variant spills
+template <int M, class R, bool SAME>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 4 : 2)
+    k_jacobi_list(OpParams P, SCoef<R> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
+                  View<const R> C, Grains<R> G, View<const R> invD, View<const R> D, View<const R> xi,
+                  View<const R> b, View<R> xo, R omega) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_node(list[t], S.lo, i, j, k);
-    jacobi_node<M, float, true, SAME>(P, K, C, G, invD, D, xi, b, xo, omega, i, j, k);
+    jacobi_node<M, R, true, SAME>(P, K, C, G, invD, D, xi, b, xo, omega, i, j, k);
 }
 
 // r = b - A x at the listed nodes (the per-node residual, k_residual's arithmetic); r may alias b
-template <int M>
-__global__ void __launch_bounds__(kBlock, 4)
-    k_residual_list(OpParams P, SCoef<float> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
-                    View<const float> C, Grains<float> G, View<const float> x, View<const float> b, View<float> r) {
+template <int M, class R>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 4 : 2)
+    k_residual_list(OpParams P, SCoef<R> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
+                    View<const R> C, Grains<R> G, View<const R> x, View<const R> b, View<R> r) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_node(list[t], S.lo, i, j, k);
-    float v[3];
+    R v[3];
     const long long ox = x.at(i, j, k);
-    apply_at<M, float, true>(P, K, C, G, x, i, j, k, ox, ox, v);
+    apply_at<M, R, true>(P, K, C, G, x, i, j, k, ox, ox, v);
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        const float rv = b.p[ox + q * x.sc] - v[q];
+        const R rv = b.p[ox + q * x.sc] - v[q];
         r.p[ox + q * x.sc] = rv;
     }
 }
@@ -442,14 +475,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // Tensor map over a level array [comp][k][j][i] (storage box, row pitch px), boxes of
-// SBW x rows x 1 x ncomp elements of 4 bytes.
-CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUtensorMapDataType type) {
+// SBW x rows x 1 x ncomp elements of esize bytes.
+CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUtensorMapDataType type, int esize) {
     const Box3 s = geo_store(g);
     const cuuint64_t nx = (cuuint64_t)(s.hi[0] - s.lo[0] + 1), ny = (cuuint64_t)(s.hi[1] - s.lo[1] + 1),
                      nz = (cuuint64_t)(s.hi[2] - s.lo[2] + 1);
     const cuuint64_t px = (cuuint64_t)g.px;
     const cuuint64_t dims[4] = {nx, ny, nz, (cuuint64_t)ncomp};
-    const cuuint64_t strides[3] = {px * 4, px * ny * 4, px * ny * nz * 4};
+    const cuuint64_t e = (cuuint64_t)esize;
+    const cuuint64_t strides[3] = {px * e, px * ny * e, px * ny * nz * e};
     const cuuint32_t box[4] = {(cuuint32_t)SBW, (cuuint32_t)rows, 1, (cuuint32_t)ncomp};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     CUtensorMap m;
@@ -460,26 +494,25 @@ CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUte
     return m;
 }
 
-// tab_n: the table's floats as padded in shared memory
-size_t tile_smem(int tab_n, bool tabs) { return sizeof(float) * (size_t)(kOffT + (tabs ? tab_n : 0)); }
-
-template <int M, bool TABS, int OP>
+template <int M, class R, bool TABS, int OP>
 void tile_smem_attr(size_t bytes) {
     static size_t set = 0;
     if (bytes > set) {
-        AE_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_tile<M, TABS, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        AE_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_tile<M, R, TABS, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes));
         set = bytes;
     }
 }
 
-// the tiled kernel of one operation over I; b: the right-hand side, invD: 1/D (Jacobi only)
-template <int OP>
-void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Box3& S, View<const float> x,
-                 const float* b, const float* invD, float* out, float omega, cudaStream_t st, Grains<float> G,
-                 int ngrains, int* err) {
-    const SCoef<float> K = make_scoef<float>(P.g);
-    dispatch_model<float>(P.model, [&](auto m) {
+// the tiled kernel of one operation over I; b: the right-hand side, invD: 1/D and D (Jacobi only;
+// D read in FP64)
+template <class R, int OP>
+void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Box3& S, View<const R> x, const R* b,
+                 const R* invD, const R* D, R* out, R omega, cudaStream_t st, Grains<R> G, int ngrains, int* err) {
+    const SCoef<R> K = make_scoef<R>(P.g);
+    const CUtensorMapDataType dt = sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    constexpr int E = (int)sizeof(R);
+    dispatch_model<R>(P.model, [&](auto m) {
         constexpr int Mv = decltype(m)::value;
         TileGeo T;
         T.I = I;
@@ -488,25 +521,27 @@ void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Bo
         T.tiles_x = (nx + STX - 1) / STX;
         const int tiles_y = (ny + STY - 1) / STY;
         T.kz = sl.kz > 0 ? sl.kz : 8;
-        // every tile starts 32 nodes after the previous one, so one shift serves all of them
-        T.sh = (I.lo[0] - 1 - S.lo[0]) & 3;
-        const CUtensorMap tx = level_tmap(x.p, P.g, 3, SXR, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-        const CUtensorMap tb = level_tmap(b, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-        const CUtensorMap td = level_tmap(invD ? invD : b, P.g, 3, STY, CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
-        const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32);
+        // every tile starts 32 nodes after the previous one, so one shift serves all of them: the
+        // boxes' first column is then 16-byte aligned (x * E a multiple of 16)
+        T.sh = (I.lo[0] - 1 - S.lo[0]) & (16 / E - 1);
+        const CUtensorMap tx = level_tmap(x.p, P.g, 3, SXR, dt, E);
+        const CUtensorMap tb = level_tmap(b, P.g, 3, STY, dt, E);
+        const CUtensorMap ti = level_tmap(invD ? invD : b, P.g, 3, STY, dt, E);
+        const CUtensorMap td = level_tmap(D ? D : b, P.g, 3, STY, dt, E);
+        const CUtensorMap tg = level_tmap(sl.gidm, P.g, 1, STY, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4);
         const dim3 grid((unsigned)(T.tiles_x * tiles_y), (unsigned)((nz + T.kz - 1) / T.kz));
         const int tab_n = ngrains * NCoef<Mv>::value;
         const int tab_pad = ngrains * ((NCoef<Mv>::value + 3) / 4 * 4);
-        const bool tabs = tab_pad * (int)sizeof(float) <= kTabSmemMax;
-        const size_t smem = tile_smem(tab_pad, tabs);
+        const bool tabs = tab_pad * E <= kTabSmemMax;
+        const size_t smem = (size_t)TL<R>::oT + (tabs ? (size_t)tab_pad * E : 0);
         if (tabs) {
-            tile_smem_attr<Mv, true, OP>(smem);
-            k_sweep_tile<Mv, true, OP><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc,
-                                                                 sl.gidm, G.tab, tab_n, out, omega, err);
+            tile_smem_attr<Mv, R, true, OP>(smem);
+            k_sweep_tile<Mv, R, true, OP><<<grid, SNT, smem, st>>>(tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz,
+                                                                    x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
         } else {
-            tile_smem_attr<Mv, false, OP>(smem);
-            k_sweep_tile<Mv, false, OP><<<grid, SNT, smem, st>>>(tx, tb, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc,
-                                                                  sl.gidm, G.tab, tab_n, out, omega, err);
+            tile_smem_attr<Mv, R, false, OP>(smem);
+            k_sweep_tile<Mv, R, false, OP><<<grid, SNT, smem, st>>>(tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz,
+                                                                     x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
         }
         launched();
     });
@@ -562,41 +597,56 @@ long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& s
     return sl.n;
 }
 
-void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
-                         View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
-                         cudaStream_t st, Grains<float> G, int ngrains, int* err) {
+template <class R>
+void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> invD, View<const R> D,
+                         View<const R> xi, View<const R> b, View<R> xo, R omega, cudaStream_t st, Grains<R> G,
+                         int ngrains, int* err) {
     const Box3 S = geo_store(P.g);
     const Box3 I = split_interior(P.g);
     const bool same = same_layout(xi, C) && same_layout(xi, invD) && same_layout(xi, D) && same_layout(xi, b) &&
                       same_layout(xi, xo);
     if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
-    if (!box_empty(I)) launch_tile<SPLIT_JACOBI>(P, sl, I, S, xi, b.p, invD.p, xo.p, omega, st, G, ngrains, err);
+    if (!box_empty(I))
+        launch_tile<R, SPLIT_JACOBI>(P, sl, I, S, xi, b.p, invD.p, sizeof(R) == 8 ? D.p : nullptr, xo.p, omega, st, G,
+                                     ngrains, err);
     if (sl.n > 0) {
-        const SCoef<float> K = make_scoef<float>(P.g);
-        dispatch_model<float>(P.model, [&](auto m) {
-            k_jacobi_list<decltype(m)::value, true><<<(unsigned)((sl.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        const SCoef<R> K = make_scoef<R>(P.g);
+        dispatch_model<R>(P.model, [&](auto m) {
+            k_jacobi_list<decltype(m)::value, R, true><<<(unsigned)((sl.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(
                 P, K, sl.list, sl.n, S, C, G, invD, D, xi, b, xo, omega);
         });
         launched();
     }
 }
 
-void launch_residual_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> x,
-                           View<const float> b, View<float> r, cudaStream_t st, Grains<float> G, int ngrains,
-                           int* err) {
+template <class R>
+void launch_residual_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> x, View<const R> b,
+                           View<R> r, cudaStream_t st, Grains<R> G, int ngrains, int* err) {
     const Box3 S = geo_store(P.g);
     const Box3 I = split_interior(P.g);
     const bool same = same_layout(x, C) && same_layout(x, b) && same_layout(x, r);
     if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
-    if (!box_empty(I)) launch_tile<SPLIT_RESIDUAL>(P, sl, I, S, x, b.p, nullptr, r.p, 0.0f, st, G, ngrains, err);
+    if (!box_empty(I))
+        launch_tile<R, SPLIT_RESIDUAL>(P, sl, I, S, x, b.p, nullptr, nullptr, r.p, R(0), st, G, ngrains, err);
     if (sl.n_r > 0) {
-        const SCoef<float> K = make_scoef<float>(P.g);
-        dispatch_model<float>(P.model, [&](auto m) {
-            k_residual_list<decltype(m)::value><<<(unsigned)((sl.n_r + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        const SCoef<R> K = make_scoef<R>(P.g);
+        dispatch_model<R>(P.model, [&](auto m) {
+            k_residual_list<decltype(m)::value, R><<<(unsigned)((sl.n_r + kBlock - 1) / kBlock), kBlock, 0, st>>>(
                 P, K, sl.list_r, sl.n_r, S, C, G, x, b, r);
         });
         launched();
     }
 }
+
+template void launch_jacobi_split<float>(const OpParams&, const SplitList&, View<const float>, View<const float>,
+                                         View<const float>, View<const float>, View<const float>, View<float>, float,
+                                         cudaStream_t, Grains<float>, int, int*);
+template void launch_jacobi_split<double>(const OpParams&, const SplitList&, View<const double>, View<const double>,
+                                          View<const double>, View<const double>, View<const double>, View<double>,
+                                          double, cudaStream_t, Grains<double>, int, int*);
+template void launch_residual_split<float>(const OpParams&, const SplitList&, View<const float>, View<const float>,
+                                           View<const float>, View<float>, cudaStream_t, Grains<float>, int, int*);
+template void launch_residual_split<double>(const OpParams&, const SplitList&, View<const double>, View<const double>,
+                                            View<const double>, View<double>, cudaStream_t, Grains<double>, int, int*);
 
 }  // namespace ae

@@ -29,14 +29,15 @@ bool split_supported(const Geo& g);
 // returns the list's length.  scratch_count: one device counter.  Synchronises the stream.
 long long split_build(const Geo& g, View<const unsigned short> gid, SplitList& sl, cudaStream_t st,
                       unsigned long long* scratch_count);
-// One damped-Jacobi sweep (FP32) of a grain-map level: the tiled interior kernel, then the list.
-// *err is set (device) when a TMA load of the tiled kernel did not complete.
-void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> invD,
-                         View<const float> D, View<const float> xi, View<const float> b, View<float> xo, float omega,
-                         cudaStream_t st, Grains<float> G, int ngrains, int* err);
-// r = b - A x (FP32) on the apply region of a grain-map level, the same split; r may alias b.
-void launch_residual_split(const OpParams& P, const SplitList& sl, View<const float> C, View<const float> x,
-                           View<const float> b, View<float> r, cudaStream_t st, Grains<float> G, int ngrains,
-                           int* err);
+// One damped-Jacobi sweep (FP32 or FP64) of a grain-map level: the tiled interior kernel, then the
+// list.  *err is set (device) when a TMA load of the tiled kernel did not complete.
+template <class R>
+void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> invD, View<const R> D,
+                         View<const R> xi, View<const R> b, View<R> xo, R omega, cudaStream_t st, Grains<R> G,
+                         int ngrains, int* err);
+// r = b - A x on the apply region of a grain-map level, the same split; r may alias b.
+template <class R>
+void launch_residual_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> x, View<const R> b,
+                           View<R> r, cudaStream_t st, Grains<R> G, int ngrains, int* err);
 
 }  // namespace ae

@@ -118,6 +118,59 @@ def test_split_sweep_mixed_solve_equals_per_node(nlev):
         assert np.array_equal(a, b)
 
 
+def _fsmooth64(op, a, L, x, b, sweeps):
+    xd = torch.from_numpy(x.astype(np.float64)).cuda()
+    bd = torch.from_numpy(b.astype(np.float64)).cuda()
+    op.Fsmooth(a, 0, Field(xd, _lo(L)), Field(bd, _lo(L)), sweeps, 2.0 / 3.0)
+    torch.cuda.synchronize()
+    return xd.cpu().numpy()
+
+
+@pytest.mark.parametrize("uniform", [False, True])
+def test_split_fp64_sweep_equals_per_node(uniform):
+    """The FP64 split sweep (the reference's damped-Jacobi update, D read from its own tile)
+    against the one-pass FP64 sweep, bit for bit: a single level and a refined patch."""
+    rng = np.random.default_rng(7)
+    Ls = [po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))]
+    gids, tab = _grains(Ls)
+    bc = bc_random(rng)
+    x = rng.standard_normal((3,) + Ls[0].shape)
+    b = rng.standard_normal((3,) + Ls[0].shape)
+    ref = _fsmooth64(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3)
+    got = _fsmooth64(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3)
+    assert np.array_equal(got, ref), int((got != ref).sum())
+    Ls, _, bc, _ = polycrystal_amr(24, 2)
+    gids, tab = _grains(Ls)
+    for a, L in enumerate(Ls):
+        x = rng.standard_normal((3,) + L.shape)
+        b = rng.standard_normal((3,) + L.shape)
+        ref = _fsmooth64(_op(False, Ls, bc, gids, tab, uniform, pad=False), a, L, x, b, 2)
+        got = _fsmooth64(_op(True, Ls, bc, gids, tab, uniform), a, L, x, b, 2)
+        assert np.array_equal(got, ref), (a, int((got != ref).sum()))
+
+
+@pytest.mark.parametrize("nlev", [1, 2])
+def test_split_fp64_solve_equals_per_node(nlev):
+    """Whole FP64 solves (every sweep and residual of the grain-map levels split) equal the
+    one-pass solves bit for bit, with the same iteration count."""
+    Ls, Cs, bc, bs = polycrystal_amr(24, nlev)
+    gids, tab = _grains(Ls)
+    out = []
+    for split in (False, True):
+        op = _op(split, Ls, bc, gids, tab, False, split)
+        s = Linear(op)
+        s.setMaxFmgIter(0)
+        s.setBottomSolver("cg")
+        s.setPrecision("fp64")
+        xs = [np.zeros_like(b) for b in bs]
+        s.solve([Field(x, _lo(L)) for x, L in zip(xs, Ls)], [Field(b, _lo(L)) for b, L in zip(bs, Ls)], 1e-8, 0.0)
+        assert s.stats.converged
+        out.append((s.stats.iters, xs))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+
+
 def test_padded_pitch_changes_no_fp64_result():
     """The FP64 solve on the padded layout equals the dense layout bit for bit."""
     Ls, Cs, bc, bs = polycrystal_amr(24, 2)
