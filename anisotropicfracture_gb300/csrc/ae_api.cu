@@ -535,6 +535,10 @@ void sweep_fapply(ae_op* op, const Geo& g, const R* C, const R* x, R* f, cudaStr
         launch_tiled<R>(0, P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                         cview(level_view(g, const_cast<R*>(x))), cview(level_view(g, const_cast<R*>(x))),
                         cview(level_view(g, const_cast<R*>(x))), level_view(g, f), R(0), st);
+    else if (const MGLevel* sl = op->split_for<R>(C))
+        launch_fapply_split<R>(P, sl->split, cview(level_view(g, const_cast<R*>(C))),
+                               cview(level_view(g, const_cast<R*>(x))), level_view(g, f), st, op->grains_for<R>(C),
+                               sl->ngrains, op->dflag + 2);
     else
         launch_fapply<R>(P, cview(level_view(g, const_cast<R*>(C))), cview(level_view(g, const_cast<R*>(x))),
                          level_view(g, f), st, op->grains_for<R>(C));
@@ -1354,7 +1358,8 @@ int ae_fapply(ae_op* op, int amrlev, int mglev, const ae_fab* out, const ae_fab*
         require(in->is_float == out->is_float, "Fapply: in and out must share a precision");
         require(is_device_ptr(in->data) && is_device_ptr(out->data), "Fapply: fabs must be device memory");
         const OpParams P = op->params(L.g);
-        // the tiled kernel works on internal buffers: stage in -> tmp, apply into rescor, copy out
+        // the tiled and split kernels work on internal buffers: stage in -> tmp, apply into rescor,
+        // copy out
         auto tiled = [&](auto zero) {
             using R = decltype(zero);
             LevelPtrs<R> p = ptrs<R>(L);
@@ -1365,12 +1370,12 @@ int ae_fapply(ae_op* op, int amrlev, int mglev, const ae_fab* out, const ae_fab*
         if (in->is_float) {
             require(op->prepared, "FP32 Fapply needs a prepared operator", AE_ERR_STATE);
             prepare32(op);
-            if (op->tiled32) tiled(0.0f);
+            if (op->tiled32 || op->split_for<float>(L.C32)) tiled(0.0f);
             else
                 launch_fapply<float>(P, cview(level_view(L.g, L.C32)), cview(fab_view<float>(*in)),
                                      fab_view<float>(*out), op->st, op->grains_for<float>(L.C32));
         } else {
-            if (op->tiled64) tiled(0.0);
+            if (op->tiled64 || op->split_for<double>(L.C)) tiled(0.0);
             else
                 launch_fapply<double>(P, cview(level_view(L.g, L.C)), cview(fab_view<double>(*in)),
                                       fab_view<double>(*out), op->st, op->grains_for<double>(L.C));

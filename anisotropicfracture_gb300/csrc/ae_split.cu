@@ -183,10 +183,10 @@ struct TileGeo {
 // One sweep over the interior box I of a grain-map level, A the interior row of
 // Elastic<T>::Fapply: OP = SPLIT_JACOBI, the damped-Jacobi update (jacobi_update: the reference's
 // form in FP64, x + w (b - A x) / D in the FP32 cycle; Operator.cpp:109-157); OP = SPLIT_RESIDUAL,
-// out = b - A x (out may alias b: every node reads only its own b).  The grain table is staged
+// out = b - A x (out may alias b: every node reads only its own b); OP = SPLIT_FAPPLY, out = A x.  The grain table is staged
 // in shared memory (TABS, rows padded to 16 bytes) or read through L1.  err: set when a TMA load
 // did not complete.
-enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1 };
+enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1, SPLIT_FAPPLY = 2 };
 template <int M, class R, bool TABS, int OP>
 __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     k_sweep_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
@@ -240,12 +240,12 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     };
     auto load_v = [&](int k, unsigned bar) {
         const unsigned s = (unsigned)(k & 1);
-        tma_load4(sb + (unsigned)L::oB + s * L::VS, &tm_b, xa, yv, k - T.slo[2], 0, bar);
+        if (OP != SPLIT_FAPPLY) tma_load4(sb + (unsigned)L::oB + s * L::VS, &tm_b, xa, yv, k - T.slo[2], 0, bar);
         if (OP == SPLIT_JACOBI) tma_load4(sb + (unsigned)L::oI + s * L::VS, &tm_i, xa, yv, k - T.slo[2], 0, bar);
         if (D64) tma_load4(sb + (unsigned)L::oD + s * L::VS, &tm_d, xa, yv, k - T.slo[2], 0, bar);
         tma_load4(sb + (unsigned)L::oG + s * L::GS, &tm_g, xa, yv, k - T.slo[2], 0, bar);
     };
-    constexpr unsigned kVTile = (OP == SPLIT_JACOBI ? (D64 ? 3 : 2) : 1) * L::kV + L::kG;
+    constexpr unsigned kVTile = (OP == SPLIT_JACOBI ? (D64 ? 3 : 2) : OP == SPLIT_RESIDUAL ? 1 : 0) * L::kV + L::kG;
     // stage 0: planes k0-1, k0, k0+1 of x and the b, 1/D (D), id tiles of plane k0
     if (leader) {
         mbar_expect_tx(bar0, 3 * L::kX + kVTile);
@@ -361,8 +361,10 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
             for (int n = 0; n < 3; ++n) {
                 if (OP == SPLIT_JACOBI)
                     xo[o + n * sc] = jacobi_update<R>(xv[n], f[n], bv[n * SVP], D64 ? dv[n * SVP] : R(0), iv[n * SVP], omega);
-                else
+                else if (OP == SPLIT_RESIDUAL)
                     xo[o + n * sc] = bv[n * SVP] - f[n];
+                else
+                    xo[o + n * sc] = f[n];
             }
         }
         __syncthreads();
@@ -412,8 +414,10 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
                 if (OP == SPLIT_JACOBI)
                     xo[qo + r * sc] = jacobi_update<R>(qc[r * SXP], fr, qb[r * SVP], D64 ? qd[r * SVP] : R(0),
                                                        qi[r * SVP], omega);
-                else
+                else if (OP == SPLIT_RESIDUAL)
                     xo[qo + r * sc] = qb[r * SVP] - fr;
+                else
+                    xo[qo + r * sc] = fr;
             }
         }
         __syncthreads();
@@ -456,6 +460,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 4 : 2)
         const R rv = b.p[ox + q * x.sc] - v[q];
         r.p[ox + q * x.sc] = rv;
     }
+}
+
+// f = A x at the listed nodes (k_fapply's arithmetic)
+template <int M, class R>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 4 : 2)
+    k_fapply_list(OpParams P, SCoef<R> K, const unsigned long long* __restrict__ list, long long n, Box3 S,
+                  View<const R> C, Grains<R> G, View<const R> x, View<R> f) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_node(list[t], S.lo, i, j, k);
+    R v[3];
+    const long long ox = x.at(i, j, k);
+    apply_at<M, R, true>(P, K, C, G, x, i, j, k, ox, ox, v);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) f.p[ox + q * x.sc] = v[q];
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
@@ -638,6 +658,28 @@ void launch_residual_split(const OpParams& P, const SplitList& sl, View<const R>
     }
 }
 
+template <class R>
+void launch_fapply_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> x, View<R> f,
+                         cudaStream_t st, Grains<R> G, int ngrains, int* err) {
+    const Box3 S = geo_store(P.g);
+    const Box3 I = split_interior(P.g);
+    const bool same = same_layout(x, C) && same_layout(x, f);
+    if (!same || !split_supported(P.g)) throw std::runtime_error("split sweep needs the level's internal arrays");
+    if (!box_empty(I)) launch_tile<R, SPLIT_FAPPLY>(P, sl, I, S, x, x.p, nullptr, nullptr, f.p, R(0), st, G, ngrains, err);
+    if (sl.n_r > 0) {
+        const SCoef<R> K = make_scoef<R>(P.g);
+        dispatch_model<R>(P.model, [&](auto m) {
+            k_fapply_list<decltype(m)::value, R><<<(unsigned)((sl.n_r + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+                P, K, sl.list_r, sl.n_r, S, C, G, x, f);
+        });
+        launched();
+    }
+}
+
+template void launch_fapply_split<float>(const OpParams&, const SplitList&, View<const float>, View<const float>,
+                                         View<float>, cudaStream_t, Grains<float>, int, int*);
+template void launch_fapply_split<double>(const OpParams&, const SplitList&, View<const double>, View<const double>,
+                                          View<double>, cudaStream_t, Grains<double>, int, int*);
 template void launch_jacobi_split<float>(const OpParams&, const SplitList&, View<const float>, View<const float>,
                                          View<const float>, View<const float>, View<const float>, View<float>, float,
                                          cudaStream_t, Grains<float>, int, int*);

@@ -35,6 +35,10 @@ template <class R>
 void launch_jacobi_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> invD, View<const R> D,
                          View<const R> xi, View<const R> b, View<R> xo, R omega, cudaStream_t st, Grains<R> G,
                          int ngrains, int* err);
+// f = A x on the apply region of a grain-map level, the same split (f other than x).
+template <class R>
+void launch_fapply_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> x, View<R> f,
+                         cudaStream_t st, Grains<R> G, int ngrains, int* err);
 // r = b - A x on the apply region of a grain-map level, the same split; r may alias b.
 template <class R>
 void launch_residual_split(const OpParams& P, const SplitList& sl, View<const R> C, View<const R> x, View<const R> b,

@@ -171,6 +171,28 @@ def test_split_fp64_solve_equals_per_node(nlev):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_split_fapply_equals_per_node(dtype):
+    """Fapply through the split kernels (staged through the level's buffers) equals the one-pass
+    per-node Fapply over the caller's fabs, bit for bit, on a single level and a refined patch."""
+    rng = np.random.default_rng(12)
+    for Ls, bc in (([po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))], bc_random(rng)),
+                   (polycrystal_amr(24, 2)[0], bc_random(rng))):
+        gids, tab = _grains(Ls)
+        for a, L in enumerate(Ls):
+            x = rng.standard_normal((3,) + L.shape).astype(dtype)
+            outs = []
+            for split in (False, True):
+                op = _op(split, Ls, bc, gids, tab, False, pad=split)
+                xd = torch.from_numpy(x).cuda()
+                fd = torch.zeros_like(xd)
+                op.Fapply(a, 0, Field(fd, _lo(L)), Field(xd, _lo(L)))
+                torch.cuda.synchronize()
+                outs.append(fd.cpu().numpy())
+                op.close()
+            assert np.array_equal(outs[0], outs[1]), (a, int((outs[0] != outs[1]).sum()))
+
+
 def test_padded_pitch_changes_no_fp64_result():
     """The FP64 solve on the padded layout equals the dense layout bit for bit."""
     Ls, Cs, bc, bs = polycrystal_amr(24, 2)
