@@ -434,15 +434,23 @@ class Newton(Linear):
         for lev in range(len(u)):
             self.linop.NewtonResidual(lev, res[lev], u[lev], b[lev], None if F0 is None else F0[lev])
 
-    def W(self, w, u, F0=None):
-        """Newton<T>::W (src/Solver/Nonlocal/Newton.H:233-275): strain energy density per node."""
+    def W(self, w, u, F0=None, model=None):
+        """Newton<T>::W (src/Solver/Nonlocal/Newton.H:233-275): strain energy density per node
+        (model: a models.NeoHookean for the finite-kinematics W(I + grad u))."""
         for lev in range(len(u)):
-            self.linop.NewtonDW(lev, u[lev], w=w[lev], F0=None if F0 is None else F0[lev])
+            if isinstance(model, NeoHookean):
+                self.linop.NeoHookeanDW(lev, u[lev], model, w=w[lev])
+            else:
+                self.linop.NewtonDW(lev, u[lev], w=w[lev], F0=None if F0 is None else F0[lev])
 
-    def DW(self, dw, u, F0=None):
-        """Newton<T>::DW (src/Solver/Nonlocal/Newton.H:277-333): DW, 9 components row-major."""
+    def DW(self, dw, u, F0=None, model=None):
+        """Newton<T>::DW (src/Solver/Nonlocal/Newton.H:277-333): DW, 9 components row-major
+        (model: a models.NeoHookean for DW(I + grad u))."""
         for lev in range(len(u)):
-            self.linop.NewtonDW(lev, u[lev], dw=dw[lev], F0=None if F0 is None else F0[lev])
+            if isinstance(model, NeoHookean):
+                self.linop.NeoHookeanDW(lev, u[lev], model, dw=dw[lev])
+            else:
+                self.linop.NewtonDW(lev, u[lev], dw=dw[lev], F0=None if F0 is None else F0[lev])
 
     def solve(self, u, b, model=None, tol_rel=None, tol_abs=None, F0=None):
         import torch

@@ -104,6 +104,12 @@ def test_dw_and_w_match_oracle():
     op.NeoHookeanDW(0, Field(_dev(u)), NEO, dw=Field(dw), w=Field(w))
     _close(_host(dw), dw_ref, "DW")
     assert normwise_err(_host(w)[0], w_ref) < TOL
+    # the Newton mirror's DW / W with the model give the same fields
+    dw2, w2 = torch.zeros_like(dw), torch.zeros_like(w)
+    s = Newton(op)
+    s.DW([Field(dw2)], [Field(_dev(u))], model=NEO)
+    s.W([Field(w2)], [Field(_dev(u))], model=NEO)
+    assert torch.equal(dw2, dw) and torch.equal(w2, w)
     op.close()
 
 
