@@ -40,6 +40,16 @@ def test_shim_uniaxial_solve():
     assert '"converged": 1' in r.stdout
 
 
+@pytest.mark.gpu
+def test_shim_neohookean_newton():
+    """Newton<Elastic::NeoHookean> from C++ (the FiniteKinematics integrator's call): the uniaxial
+    stretch lands on the exact homogeneous finite-strain solution."""
+    build.build()
+    exe = _compile("neohookean_shim.cpp", "neohookean_shim", link=True)
+    r = subprocess.run([exe, "8"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
 def test_shim_writes_a_plotfile_without_a_gpu(tmp_path):
     """alamo::WritePlotFile (host fabs only) from C++: the reference's directory naming and .visit
     list, and the valid-box values of each level read back."""
