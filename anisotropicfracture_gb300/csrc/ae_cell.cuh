@@ -66,7 +66,7 @@ __device__ __forceinline__ void cell_gradC(const SCoef<R>& K, const R* __restric
     gradC_col_f<M, R>([&](int q) { return ldv<LDG>(c0 + q * cs + o.yp) - ldv<LDG>(c0 + q * cs + o.ym); }, g, 1, c_y);
     gradC_col_f<M, R>([&](int q) { return ldv<LDG>(c0 + q * cs + o.zp) - ldv<LDG>(c0 + q * cs + o.zm); }, g, 2, c_z);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) out[r] = (c_x[r] * K.h[0] + c_y[r] * K.h[1]) + c_z[r] * K.h[2];
+    for (int r = 0; r < 3; ++r) out[r] = gradc_sum(c_x[r], c_y[r], c_z[r], K.h);
 }
 
 // f = A u at node t of a periodic cell
@@ -124,7 +124,7 @@ __device__ __forceinline__ void cell_apply_grains(const SCoef<R>& K, bool unifor
             }
         }
 #pragma unroll
-        for (int r = 0; r < 3; ++r) f[r] += (col[0][r] * K.h[0] + col[1][r] * K.h[1]) + col[2][r] * K.h[2];
+        for (int r = 0; r < 3; ++r) f[r] = gradc_add(f[r], col[0][r], col[1][r], col[2][r], K.h);
     }
 }
 

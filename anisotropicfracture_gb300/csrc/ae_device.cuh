@@ -29,6 +29,46 @@ __host__ __device__ constexpr int major_slot(int I, int K) {
     return I <= K ? I * 9 - I * (I - 1) / 2 + (K - I) : K * 9 - K * (K - 1) / 2 + (I - K);
 }
 
+// FP32 rows in one fixed rounding order.  The compiler fuses a product into a neighbouring
+// addition at its own discretion, and the choice can differ between kernels that inline the same
+// expression in different surroundings.  The FP32 operator's sums of products therefore go through
+// explicitly rounded operations -- additions rounded, the first product of a sum rounded and each
+// further one fused into the running sum -- so that every FP32 kernel computes a node's row to the
+// same bits.  FP64 keeps the written expressions.
+__device__ __forceinline__ float fx_sop_acc(float r) { return r; }
+template <class... T>
+__device__ __forceinline__ float fx_sop_acc(float r, float a, float x, T... rest) {
+    return fx_sop_acc(__fmaf_rn(a, x, r), rest...);
+}
+// a0 x0 + a1 x1 + ... in that order
+template <class... T>
+__device__ __forceinline__ float fx_sop(float a, float x, T... rest) {
+    return fx_sop_acc(__fmul_rn(a, x), rest...);
+}
+template <class R>
+__device__ __forceinline__ R add2(R x, R y) {
+    if constexpr (sizeof(R) == 4) return __fadd_rn(x, y);
+    else return x + y;
+}
+// a0 x0 + ... + a5 x5 (one row of a MajorMinor contraction)
+template <class R>
+__device__ __forceinline__ R sop6(R a0, R x0, R a1, R x1, R a2, R x2, R a3, R x3, R a4, R x4, R a5, R x5) {
+    if constexpr (sizeof(R) == 4) return fx_sop(a0, x0, a1, x1, a2, x2, a3, x3, a4, x4, a5, x5);
+    else return a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3 + a4 * x4 + a5 * x5;
+}
+// (c0 h0 + c1 h1) + c2 h2: the grad C columns of a row scaled by the central-difference factors
+template <class R>
+__device__ __forceinline__ R gradc_sum(R c0, R c1, R c2, const R h[3]) {
+    if constexpr (sizeof(R) == 4) return fx_sop(c0, h[0], c1, h[1], c2, h[2]);
+    else return (c0 * h[0] + c1 * h[1]) + c2 * h[2];
+}
+// f + the grad C term of the row
+template <class R>
+__device__ __forceinline__ R gradc_add(R f, R c0, R c1, R c2, const R h[3]) {
+    if constexpr (sizeof(R) == 4) return __fadd_rn(f, gradc_sum(c0, c1, c2, h));
+    else return f + ((c0 * h[0] + c1 * h[1]) + c2 * h[2]);
+}
+
 enum BCType { DISP = 0, TRAC = 1, PERIODIC = 2, NEUMANN = 3 };
 
 struct Box3 {
@@ -159,6 +199,34 @@ __device__ __forceinline__ void stress_of(const R* a, const R g[3][3], R s[3][3]
 template <class R>
 __device__ __forceinline__ void div_mm(const R* a, const R b[3][3][3], R f[3]) {
 #define B(p, q, r) b[p][q][r]
+    if constexpr (sizeof(R) == 4) {
+        // the same terms in the same order, explicitly rounded
+#define S2(x, y) __fadd_rn(x, y)
+#define S3(x, y, z) __fadd_rn(__fadd_rn(x, y), z)
+#define S4(x, y, z, w) __fadd_rn(__fadd_rn(__fadd_rn(x, y), z), w)
+        f[0] = fx_sop(a[0], B(0, 0, 0), a[1], S3(B(0, 1, 0), B(1, 0, 0), B(0, 0, 1)),
+                      a[2], S3(B(0, 2, 0), B(2, 0, 0), B(0, 0, 2)), a[3], B(1, 1, 0), a[4], S2(B(1, 2, 0), B(2, 1, 0)),
+                      a[5], B(2, 2, 0), a[6], S2(B(0, 1, 1), B(1, 0, 1)),
+                      a[7], S4(B(0, 2, 1), B(2, 0, 1), B(0, 1, 2), B(1, 0, 2)), a[8], B(1, 1, 1),
+                      a[9], S2(B(1, 2, 1), B(2, 1, 1)), a[10], B(2, 2, 1), a[11], S2(B(0, 2, 2), B(2, 0, 2)),
+                      a[12], B(1, 1, 2), a[13], S2(B(1, 2, 2), B(2, 1, 2)), a[14], B(2, 2, 2));
+        f[1] = fx_sop(a[1], B(0, 0, 0), a[4], B(0, 0, 2), a[3], B(0, 0, 1), a[6], S2(B(0, 1, 0), B(1, 0, 0)),
+                      a[7], S2(B(0, 2, 0), B(2, 0, 0)), a[8], S3(B(1, 1, 0), B(0, 1, 1), B(1, 0, 1)),
+                      a[9], S4(B(1, 2, 0), B(2, 1, 0), B(0, 1, 2), B(1, 0, 2)), a[10], B(2, 2, 0),
+                      a[12], S2(B(0, 2, 1), B(2, 0, 1)), a[13], S2(B(0, 2, 2), B(2, 0, 2)), a[15], B(1, 1, 1),
+                      a[16], S3(B(1, 2, 1), B(2, 1, 1), B(1, 1, 2)), a[17], B(2, 2, 1), a[18], S2(B(1, 2, 2), B(2, 1, 2)),
+                      a[19], B(2, 2, 2));
+        f[2] = fx_sop(a[2], B(0, 0, 0), a[4], B(0, 0, 1), a[5], B(0, 0, 2), a[7], S2(B(0, 1, 0), B(1, 0, 0)),
+                      a[9], S2(B(0, 1, 1), B(1, 0, 1)), a[10], S2(B(0, 1, 2), B(1, 0, 2)),
+                      a[11], S2(B(0, 2, 0), B(2, 0, 0)), a[12], B(1, 1, 0),
+                      a[13], S4(B(1, 2, 0), B(2, 1, 0), B(0, 2, 1), B(2, 0, 1)),
+                      a[14], S3(B(2, 2, 0), B(0, 2, 2), B(2, 0, 2)), a[16], B(1, 1, 1), a[17], B(1, 1, 2),
+                      a[18], S2(B(1, 2, 1), B(2, 1, 1)), a[19], S3(B(2, 2, 1), B(1, 2, 2), B(2, 1, 2)), a[20], B(2, 2, 2));
+#undef S2
+#undef S3
+#undef S4
+        return;
+    }
     f[0] = a[0] * B(0, 0, 0) + a[1] * (B(0, 1, 0) + B(1, 0, 0) + B(0, 0, 1)) +
            a[2] * (B(0, 2, 0) + B(2, 0, 0) + B(0, 0, 2)) + a[3] * B(1, 1, 0) + a[4] * (B(1, 2, 0) + B(2, 1, 0)) +
            a[5] * B(2, 2, 0) + a[6] * (B(0, 1, 1) + B(1, 0, 1)) +
@@ -247,25 +315,25 @@ __device__ __forceinline__ void gradC_col(const R* __restrict__ C, long long cs,
 #define DC(q) (ldv<LDG>(C + (q) * cs + c + o) - ldv<LDG>(C + (q) * cs + c - o))
     if (M == MM) {
         const R e00 = g[0][0], e11 = g[1][1], e22 = g[2][2];
-        const R e01 = g[0][1] + g[1][0], e02 = g[0][2] + g[2][0], e12 = g[1][2] + g[2][1];
+        const R e01 = add2(g[0][1], g[1][0]), e02 = add2(g[0][2], g[2][0]), e12 = add2(g[1][2], g[2][1]);
         if (d == 0) {  // (s00, s01, s20)
             const R a0 = DC(0), a1 = DC(1), a2 = DC(2), a3 = DC(3), a4 = DC(4), a5 = DC(5), a6 = DC(6), a7 = DC(7);
             const R a8 = DC(8), a9 = DC(9), a10 = DC(10), a11 = DC(11), a12 = DC(12), a13 = DC(13), a14 = DC(14);
-            col[0] = a0 * e00 + a1 * e01 + a2 * e02 + a3 * e11 + a4 * e12 + a5 * e22;
-            col[1] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
-            col[2] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
+            col[0] = sop6(a0, e00, a1, e01, a2, e02, a3, e11, a4, e12, a5, e22);
+            col[1] = sop6(a1, e00, a6, e01, a7, e02, a8, e11, a9, e12, a10, e22);
+            col[2] = sop6(a2, e00, a7, e01, a11, e02, a12, e11, a13, e12, a14, e22);
         } else if (d == 1) {  // (s01, s11, s12)
             const R a1 = DC(1), a3 = DC(3), a4 = DC(4), a6 = DC(6), a7 = DC(7), a8 = DC(8), a9 = DC(9), a10 = DC(10);
             const R a12 = DC(12), a13 = DC(13), a15 = DC(15), a16 = DC(16), a17 = DC(17), a18 = DC(18), a19 = DC(19);
-            col[0] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
-            col[1] = a3 * e00 + a8 * e01 + a12 * e02 + a15 * e11 + a16 * e12 + a17 * e22;
-            col[2] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
+            col[0] = sop6(a1, e00, a6, e01, a7, e02, a8, e11, a9, e12, a10, e22);
+            col[1] = sop6(a3, e00, a8, e01, a12, e02, a15, e11, a16, e12, a17, e22);
+            col[2] = sop6(a4, e00, a9, e01, a13, e02, a16, e11, a18, e12, a19, e22);
         } else {  // (s20, s12, s22)
             const R a2 = DC(2), a4 = DC(4), a5 = DC(5), a7 = DC(7), a9 = DC(9), a10 = DC(10), a11 = DC(11), a12 = DC(12);
             const R a13 = DC(13), a14 = DC(14), a16 = DC(16), a17 = DC(17), a18 = DC(18), a19 = DC(19), a20 = DC(20);
-            col[0] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
-            col[1] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
-            col[2] = a5 * e00 + a10 * e01 + a14 * e02 + a17 * e11 + a19 * e12 + a20 * e22;
+            col[0] = sop6(a2, e00, a7, e01, a11, e02, a12, e11, a13, e12, a14, e22);
+            col[1] = sop6(a4, e00, a9, e01, a13, e02, a16, e11, a18, e12, a19, e22);
+            col[2] = sop6(a5, e00, a10, e01, a14, e02, a17, e11, a19, e12, a20, e22);
         }
     } else if (M == MAJOR) {
 #pragma unroll
@@ -306,25 +374,25 @@ template <int M, class R, class F>
 __device__ __forceinline__ void gradC_col_f(F&& dC, const R g[3][3], int d, R col[3]) {
     if (M == MM) {
         const R e00 = g[0][0], e11 = g[1][1], e22 = g[2][2];
-        const R e01 = g[0][1] + g[1][0], e02 = g[0][2] + g[2][0], e12 = g[1][2] + g[2][1];
+        const R e01 = add2(g[0][1], g[1][0]), e02 = add2(g[0][2], g[2][0]), e12 = add2(g[1][2], g[2][1]);
         if (d == 0) {
             const R a0 = dC(0), a1 = dC(1), a2 = dC(2), a3 = dC(3), a4 = dC(4), a5 = dC(5), a6 = dC(6), a7 = dC(7);
             const R a8 = dC(8), a9 = dC(9), a10 = dC(10), a11 = dC(11), a12 = dC(12), a13 = dC(13), a14 = dC(14);
-            col[0] = a0 * e00 + a1 * e01 + a2 * e02 + a3 * e11 + a4 * e12 + a5 * e22;
-            col[1] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
-            col[2] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
+            col[0] = sop6(a0, e00, a1, e01, a2, e02, a3, e11, a4, e12, a5, e22);
+            col[1] = sop6(a1, e00, a6, e01, a7, e02, a8, e11, a9, e12, a10, e22);
+            col[2] = sop6(a2, e00, a7, e01, a11, e02, a12, e11, a13, e12, a14, e22);
         } else if (d == 1) {
             const R a1 = dC(1), a3 = dC(3), a4 = dC(4), a6 = dC(6), a7 = dC(7), a8 = dC(8), a9 = dC(9), a10 = dC(10);
             const R a12 = dC(12), a13 = dC(13), a15 = dC(15), a16 = dC(16), a17 = dC(17), a18 = dC(18), a19 = dC(19);
-            col[0] = a1 * e00 + a6 * e01 + a7 * e02 + a8 * e11 + a9 * e12 + a10 * e22;
-            col[1] = a3 * e00 + a8 * e01 + a12 * e02 + a15 * e11 + a16 * e12 + a17 * e22;
-            col[2] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
+            col[0] = sop6(a1, e00, a6, e01, a7, e02, a8, e11, a9, e12, a10, e22);
+            col[1] = sop6(a3, e00, a8, e01, a12, e02, a15, e11, a16, e12, a17, e22);
+            col[2] = sop6(a4, e00, a9, e01, a13, e02, a16, e11, a18, e12, a19, e22);
         } else {
             const R a2 = dC(2), a4 = dC(4), a5 = dC(5), a7 = dC(7), a9 = dC(9), a10 = dC(10), a11 = dC(11), a12 = dC(12);
             const R a13 = dC(13), a14 = dC(14), a16 = dC(16), a17 = dC(17), a18 = dC(18), a19 = dC(19), a20 = dC(20);
-            col[0] = a2 * e00 + a7 * e01 + a11 * e02 + a12 * e11 + a13 * e12 + a14 * e22;
-            col[1] = a4 * e00 + a9 * e01 + a13 * e02 + a16 * e11 + a18 * e12 + a19 * e22;
-            col[2] = a5 * e00 + a10 * e01 + a14 * e02 + a17 * e11 + a19 * e12 + a20 * e22;
+            col[0] = sop6(a2, e00, a7, e01, a11, e02, a12, e11, a13, e12, a14, e22);
+            col[1] = sop6(a4, e00, a9, e01, a13, e02, a16, e11, a18, e12, a19, e22);
+            col[2] = sop6(a5, e00, a10, e01, a14, e02, a17, e11, a19, e12, a20, e22);
         }
     } else if (M == MAJOR) {
 #pragma unroll
@@ -465,7 +533,7 @@ __device__ __forceinline__ void apply_node(const Geo& g, const SCoef<R>& K, cons
         gradC_col<M, R, LDG>(C, cs, cc, csy, gu, 1, c1);
         gradC_col<M, R, LDG>(C, cs, cc, csz, gu, 2, c2);
 #pragma unroll
-        for (int r = 0; r < 3; ++r) f[r] += (c0[r] * K.h[0] + c1[r] * K.h[1]) + c2[r] * K.h[2];
+        for (int r = 0; r < 3; ++r) f[r] = gradc_add(f[r], c0[r], c1[r], c2[r], K.h);
     }
 }
 
@@ -558,7 +626,7 @@ __device__ __forceinline__ void apply_node_grains(const Geo& g, const SCoef<R>& 
             }
         }
 #pragma unroll
-        for (int r = 0; r < 3; ++r) f[r] += (col[0][r] * K.h[0] + col[1][r] * K.h[1]) + col[2][r] * K.h[2];
+        for (int r = 0; r < 3; ++r) f[r] = gradc_add(f[r], col[0][r], col[1][r], col[2][r], K.h);
     }
 }
 

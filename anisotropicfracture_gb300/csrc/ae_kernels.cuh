@@ -182,8 +182,9 @@ __device__ __forceinline__ double jacobi_update_impl(double xv, double ax, doubl
     return (1.0 - omega) * xv + omega * (b - rx) * invd;
 }
 __device__ __forceinline__ float jacobi_update_impl(float xv, float ax, float b, float, float invd, float omega) {
-    // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D
-    return xv + omega * (b - ax) * invd;
+    // FP32 cycle: the same update written x + w (b - Ax) / D, which reads no D (rounded in one
+    // fixed order, as the FP32 rows are)
+    return __fmaf_rn(__fmul_rn(omega, __fsub_rn(b, ax)), invd, xv);
 }
 template <class R>
 __device__ __forceinline__ R jacobi_update(R xv, R ax, R b, R d, R invd, R omega) {
@@ -427,7 +428,7 @@ __global__ void __launch_bounds__(TX* TY, 2) k_tiled(OpParams P, SCoef<R> K, Box
                         gradC_col_f<M, R>([&](int q) { return Cn[q * HP + idx] - Cm[zslot_index<M>(q)]; }, gu, 2,
                                           c2v);
 #pragma unroll
-                        for (int r = 0; r < 3; ++r) f[r] += (c0v[r] * K.h[0] + c1v[r] * K.h[1]) + c2v[r] * K.h[2];
+                        for (int r = 0; r < 3; ++r) f[r] = gradc_add(f[r], c0v[r], c1v[r], c2v[r], K.h);
                     }
                 }
                 if (OP == OP_FAPPLY) {

@@ -49,6 +49,14 @@ constexpr int kWaitLimit = 1 << 20;        // try_wait polls before a wait is de
 #ifndef AE_SPLIT_MIN_BLOCKS
 #define AE_SPLIT_MIN_BLOCKS 4
 #endif
+// FP32: each thread computes the nodes of NPT consecutive rows (j, j + 1), which share the loads
+// of two rows of every plane: 28 instead of 38 shared-memory loads per component per pair
+#ifndef AE_SPLIT_NPT32
+#define AE_SPLIT_NPT32 2
+#endif
+#ifndef AE_SPLIT_PAIR_BLOCKS
+#define AE_SPLIT_PAIR_BLOCKS 5
+#endif
 
 __host__ __device__ constexpr int up128(int b) { return (b + 127) / 128 * 128; }
 __host__ __device__ constexpr int up16(int b) { return (b + 15) / 16 * 16; }
@@ -185,15 +193,20 @@ struct TileGeo {
 // form in FP64, x + w (b - A x) / D in the FP32 cycle; Operator.cpp:109-157); OP = SPLIT_RESIDUAL,
 // out = b - A x (out may alias b: every node reads only its own b); OP = SPLIT_FAPPLY, out = A x.  The grain table is staged
 // in shared memory (TABS, rows padded to 16 bytes) or read through L1.  err: set when a TMA load
-// did not complete.
+// did not complete.  NPT: rows of the tile per thread (1, or 2: the thread's two nodes (i, j) and
+// (i, j + 1) take the x values of rows j - 1 .. j + 2 from one set of loads; each node's
+// arithmetic is unchanged).
 enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1, SPLIT_FAPPLY = 2 };
-template <int M, class R, bool TABS, int OP>
-__global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
+template <int M, class R, bool TABS, int OP, int NPT>
+__global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     k_sweep_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
                  const __grid_constant__ CUtensorMap tm_i, const __grid_constant__ CUtensorMap tm_d,
                  const __grid_constant__ CUtensorMap tm_g, SCoef<R> K, TileGeo T, int uniform, long long sy,
                  long long sz, long long sc, const unsigned* __restrict__ gidm_g, const R* __restrict__ tab, int tab_n,
                  R* __restrict__ xo, R omega, int* err) {
+    static_assert(NPT == 1 || NPT == 2, "one or two rows per thread");
+    static_assert(STY % NPT == 0, "whole row pairs per tile");
+    constexpr int NT = SNT / NPT;  // threads per block
     using L = TL<R>;
     constexpr int NC = NCoef<M>::value;
     // grain rows in shared memory padded to whole 16-byte vectors (four coefficients)
@@ -210,18 +223,19 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     if (TABS) {
         R* ts = reinterpret_cast<R*>(smem + L::oT);
         const int rows = tab_n / NC;
-        for (int q = threadIdx.x; q < rows * NCP; q += SNT) {
+        for (int q = threadIdx.x; q < rows * NCP; q += NT) {
             const int g = q / NCP, c = q - g * NCP;
             ts[q] = c < NC ? __ldg(tab + g * NC + c) : R(0);
         }
         tb = ts;
     }
-    const int tx = threadIdx.x % STX, ty = threadIdx.x / STX;
+    const int tx = threadIdx.x % STX, ty = NPT * (threadIdx.x / STX);  // the thread's first row
     const int i0 = T.I.lo[0] + (int)(blockIdx.x % T.tiles_x) * STX, j0 = T.I.lo[1] + (int)(blockIdx.x / T.tiles_x) * STY;
     const int k0 = T.I.lo[2] + (int)blockIdx.y * T.kz;
     const int k1 = min(k0 + T.kz - 1, T.I.hi[2]);
     const int i = i0 + tx, j = j0 + ty;
     const bool act = i <= T.I.hi[0] && j <= T.I.hi[1];
+    const bool act1 = NPT == 2 && i <= T.I.hi[0] && j + 1 <= T.I.hi[1];  // the second node (implies act)
     // tensor coordinates of the boxes
     const int xa = i0 - 1 - T.slo[0] - T.sh;
     const int yx = j0 - 1 - T.slo[1], yv = j0 - T.slo[1];
@@ -286,91 +300,155 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
         const R* bv = reinterpret_cast<const R*>(smem + L::oB + vs * L::VS) + cv;
         const R* iv = reinterpret_cast<const R*>(smem + L::oI + vs * L::VS) + cv;
         const R* dv = reinterpret_cast<const R*>(smem + L::oD + vs * L::VS) + cv;
-        bool queued = false;
-        R f[3], xv[3];
-        if (act) {
-            const unsigned gw = gring[vs * SVP + cv];
-            R bb[3][3][3];
+        bool queued[NPT];
+        R f[NPT][3], xv[NPT][3];
+        // the 21 (9, 2, 45) coefficients of a node's grain, then its interior term div(C : grad grad x)
+        auto interior = [&](unsigned gw, const R (&bb)[3][3][3], R (&fo)[3]) {
+            R a[NCP];
+            const R* a0 = tb + (int)(gw & 0xffffu) * TS;
+            if (TABS) {
+                if (sizeof(R) == 4) {
 #pragma unroll
-            for (int p = 0; p < 3; ++p) {
-                const R* um = pm + p * SXP;
-                const R* uc = pc + p * SXP;
-                const R* up = pp + p * SXP;
-                const R c0 = uc[0];
-                xv[p] = c0;
-                const R xm = uc[-1], xp = uc[1], ym = uc[-SBW], yp = uc[SBW], zm = um[0], zp = up[0];
-                bb[p][0][0] = (xp - R(2) * c0 + xm) * K.i2[0];
-                bb[p][1][1] = (yp - R(2) * c0 + ym) * K.i2[1];
-                bb[p][2][2] = (zp - R(2) * c0 + zm) * K.i2[2];
-                bb[p][0][1] = (uc[1 + SBW] + uc[-1 - SBW] - uc[1 - SBW] - uc[-1 + SBW]) * K.m01;
-                bb[p][0][2] = (up[1] + um[-1] - um[1] - up[-1]) * K.m02;
-                bb[p][1][2] = (up[SBW] + um[-SBW] - um[SBW] - up[-SBW]) * K.m12;
-                bb[p][1][0] = bb[p][0][1];
-                bb[p][2][0] = bb[p][0][2];
-                bb[p][2][1] = bb[p][1][2];
-            }
-            {
-                R a[NCP];
-                const R* a0 = tb + (int)(gw & 0xffffu) * TS;
-                if (TABS) {
-                    if (sizeof(R) == 4) {
-#pragma unroll
-                        for (int q = 0; q < NCP; q += 4) {
-                            const float4 v = *reinterpret_cast<const float4*>(a0 + q);
-                            a[q] = (R)v.x;
-                            a[q + 1] = (R)v.y;
-                            a[q + 2] = (R)v.z;
-                            a[q + 3] = (R)v.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < NCP; q += 2) {
-                            const double2 v = *reinterpret_cast<const double2*>(a0 + q);
-                            a[q] = (R)v.x;
-                            a[q + 1] = (R)v.y;
-                        }
+                    for (int q = 0; q < NCP; q += 4) {
+                        const float4 v = *reinterpret_cast<const float4*>(a0 + q);
+                        a[q] = (R)v.x;
+                        a[q + 1] = (R)v.y;
+                        a[q + 2] = (R)v.z;
+                        a[q + 3] = (R)v.w;
                     }
                 } else {
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) a[q] = a0[q];
+                    for (int q = 0; q < NCP; q += 2) {
+                        const double2 v = *reinterpret_cast<const double2*>(a0 + q);
+                        a[q] = (R)v.x;
+                        a[q + 1] = (R)v.y;
+                    }
                 }
-                div_of<M, R>(a, bb, f);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NC; ++q) a[q] = a0[q];
             }
-            queued = !uniform && (gw >> 16) != 0;
+            div_of<M, R>(a, bb, fo);
+        };
+        if constexpr (NPT == 1) {
+            queued[0] = false;
+            if (act) {
+                const unsigned gw = gring[vs * SVP + cv];
+                R bb[3][3][3];
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {
+                    const R* um = pm + p * SXP;
+                    const R* uc = pc + p * SXP;
+                    const R* up = pp + p * SXP;
+                    const R c0 = uc[0];
+                    xv[0][p] = c0;
+                    const R xm = uc[-1], xp = uc[1], ym = uc[-SBW], yp = uc[SBW], zm = um[0], zp = up[0];
+                    bb[p][0][0] = (xp - R(2) * c0 + xm) * K.i2[0];
+                    bb[p][1][1] = (yp - R(2) * c0 + ym) * K.i2[1];
+                    bb[p][2][2] = (zp - R(2) * c0 + zm) * K.i2[2];
+                    bb[p][0][1] = (uc[1 + SBW] + uc[-1 - SBW] - uc[1 - SBW] - uc[-1 + SBW]) * K.m01;
+                    bb[p][0][2] = (up[1] + um[-1] - um[1] - up[-1]) * K.m02;
+                    bb[p][1][2] = (up[SBW] + um[-SBW] - um[SBW] - up[-SBW]) * K.m12;
+                    bb[p][1][0] = bb[p][0][1];
+                    bb[p][2][0] = bb[p][0][2];
+                    bb[p][2][1] = bb[p][1][2];
+                }
+                interior(gw, bb, f[0]);
+                queued[0] = !uniform && (gw >> 16) != 0;
+            }
+        } else {
+            queued[0] = queued[1] = false;
+            if (act) {
+                // per component: plane k at rows j - 1 .. j + 2 and columns i - 1 .. i + 1 (12
+                // loads); planes k -+ 1 at rows j, j + 1 (three columns) and rows j - 1, j + 2
+                // (column i) (8 loads each).  Row r of these arrays is row j - 1 + r.
+                R h[2][3][6];
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {
+                    const R* um = pm + p * SXP;
+                    const R* uc = pc + p * SXP;
+                    const R* up = pp + p * SXP;
+                    R ac[4][3], am[4][3], ap[4][3];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            ac[r][c] = uc[(r - 1) * SBW + c - 1];
+                            const bool need = (r == 1 || r == 2) || c == 1;
+                            am[r][c] = need ? um[(r - 1) * SBW + c - 1] : R(0);
+                            ap[r][c] = need ? up[(r - 1) * SBW + c - 1] : R(0);
+                        }
+#pragma unroll
+                    for (int n = 0; n < 2; ++n) {
+                        const R c0 = ac[n + 1][1];
+                        xv[n][p] = c0;
+                        const R xm = ac[n + 1][0], xp = ac[n + 1][2], ym = ac[n][1], yp = ac[n + 2][1];
+                        const R zm = am[n + 1][1], zp = ap[n + 1][1];
+                        h[n][p][0] = (xp - R(2) * c0 + xm) * K.i2[0];
+                        h[n][p][1] = (yp - R(2) * c0 + ym) * K.i2[1];
+                        h[n][p][2] = (zp - R(2) * c0 + zm) * K.i2[2];
+                        h[n][p][3] = (ac[n + 2][2] + ac[n][0] - ac[n][2] - ac[n + 2][0]) * K.m01;
+                        h[n][p][4] = (ap[n + 1][2] + am[n + 1][0] - am[n + 1][2] - ap[n + 1][0]) * K.m02;
+                        h[n][p][5] = (ap[n + 2][1] + am[n][1] - am[n + 2][1] - ap[n][1]) * K.m12;
+                    }
+                }
+#pragma unroll
+                for (int n = 0; n < 2; ++n) {
+                    if (n == 1 && !act1) break;
+                    const unsigned gw = gring[vs * SVP + cv + n * SBW];
+                    R bb[3][3][3];
+#pragma unroll
+                    for (int p = 0; p < 3; ++p) {
+                        bb[p][0][0] = h[n][p][0];
+                        bb[p][1][1] = h[n][p][1];
+                        bb[p][2][2] = h[n][p][2];
+                        bb[p][0][1] = bb[p][1][0] = h[n][p][3];
+                        bb[p][0][2] = bb[p][2][0] = h[n][p][4];
+                        bb[p][1][2] = bb[p][2][1] = h[n][p][5];
+                    }
+                    interior(gw, bb, f[n]);
+                    queued[n] = !uniform && (gw >> 16) != 0;
+                }
+            }
         }
-        // nodes with a grad C column go to the plane's queue (one shared-memory atomic per warp);
-        // the others are finished here
-        {
-            const unsigned ball = __ballot_sync(0xffffffffu, queued);
-            int base = 0;
+        // nodes with a grad C column go to the plane's queue (one shared-memory atomic per warp
+        // and row); the others are finished here
+#pragma unroll
+        for (int n = 0; n < NPT; ++n) {
+            const bool an = n == 0 ? act : act1;
+            const unsigned ball = __ballot_sync(0xffffffffu, queued[n]);
             if (ball) {
                 const int lane = threadIdx.x & 31;
+                int base = 0;
                 if (lane == __ffs(ball) - 1) base = atomicAdd(qn, __popc(ball));
                 base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
-                if (queued) {
+                if (queued[n]) {
                     const int e = base + __popc(ball & ((1u << lane) - 1u));
-                    qtid[e] = (int)threadIdx.x;
-                    qf[3 * e] = f[0];
-                    qf[3 * e + 1] = f[1];
-                    qf[3 * e + 2] = f[2];
+                    qtid[e] = (ty + n) * STX + tx;  // the node's place in the tile
+                    qf[3 * e] = f[n][0];
+                    qf[3 * e + 1] = f[n][1];
+                    qf[3 * e + 2] = f[n][2];
                 }
             }
-        }
-        if (act && !queued) {
+            if (an && !queued[n]) {
+                const long long on = o + n * sy;
+                const int vn = n * SBW;
 #pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                if (OP == SPLIT_JACOBI)
-                    xo[o + n * sc] = jacobi_update<R>(xv[n], f[n], bv[n * SVP], D64 ? dv[n * SVP] : R(0), iv[n * SVP], omega);
-                else if (OP == SPLIT_RESIDUAL)
-                    xo[o + n * sc] = bv[n * SVP] - f[n];
-                else
-                    xo[o + n * sc] = f[n];
+                for (int r = 0; r < 3; ++r) {
+                    if (OP == SPLIT_JACOBI)
+                        xo[on + r * sc] = jacobi_update<R>(xv[n][r], f[n][r], bv[vn + r * SVP],
+                                                           D64 ? dv[vn + r * SVP] : R(0), iv[vn + r * SVP], omega);
+                    else if (OP == SPLIT_RESIDUAL)
+                        xo[on + r * sc] = bv[vn + r * SVP] - f[n][r];
+                    else
+                        xo[on + r * sc] = f[n][r];
+                }
             }
         }
         __syncthreads();
         // the queued nodes, one per thread: grad C columns of the directions whose neighbours lie in
         // different grains, then the update
-        for (int e = threadIdx.x; e < *qn; e += SNT) {
+        for (int e = threadIdx.x; e < *qn; e += NT) {
             const int t = qtid[e];
             const int qx = t % STX, qy = t / STX;
             const int qcx = (qy + 1) * SBW + T.sh + 1 + qx, qcv = qy * SBW + T.sh + 1 + qx;
@@ -410,7 +488,7 @@ __global__ void __launch_bounds__(SNT, sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 R fr = qf[3 * e + r];
-                fr += (colv[0][r] * K.h[0] + colv[1][r] * K.h[1]) + colv[2][r] * K.h[2];
+                fr = gradc_add(fr, colv[0][r], colv[1][r], colv[2][r], K.h);
                 if (OP == SPLIT_JACOBI)
                     xo[qo + r * sc] = jacobi_update<R>(qc[r * SXP], fr, qb[r * SVP], D64 ? qd[r * SVP] : R(0),
                                                        qi[r * SVP], omega);
@@ -514,12 +592,12 @@ CUtensorMap level_tmap(const void* base, const Geo& g, int ncomp, int rows, CUte
     return m;
 }
 
-template <int M, class R, bool TABS, int OP>
+template <int M, class R, bool TABS, int OP, int NPT>
 void tile_smem_attr(size_t bytes) {
     static size_t set = 0;
     if (bytes > set) {
-        AE_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_tile<M, R, TABS, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)bytes));
+        AE_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_tile<M, R, TABS, OP, NPT>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         set = bytes;
     }
 }
@@ -554,14 +632,15 @@ void launch_tile(const OpParams& P, const SplitList& sl, const Box3& I, const Bo
         const int tab_pad = ngrains * ((NCoef<Mv>::value + 3) / 4 * 4);
         const bool tabs = tab_pad * E <= kTabSmemMax;
         const size_t smem = (size_t)TL<R>::oT + (tabs ? (size_t)tab_pad * E : 0);
+        constexpr int NPT = E == 4 ? AE_SPLIT_NPT32 : 1;
         if (tabs) {
-            tile_smem_attr<Mv, R, true, OP>(smem);
-            k_sweep_tile<Mv, R, true, OP><<<grid, SNT, smem, st>>>(tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz,
-                                                                    x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
+            tile_smem_attr<Mv, R, true, OP, NPT>(smem);
+            k_sweep_tile<Mv, R, true, OP, NPT><<<grid, SNT / NPT, smem, st>>>(
+                tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
         } else {
-            tile_smem_attr<Mv, R, false, OP>(smem);
-            k_sweep_tile<Mv, R, false, OP><<<grid, SNT, smem, st>>>(tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz,
-                                                                     x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
+            tile_smem_attr<Mv, R, false, OP, NPT>(smem);
+            k_sweep_tile<Mv, R, false, OP, NPT><<<grid, SNT / NPT, smem, st>>>(
+                tx, tb, ti, td, tg, K, T, P.uniform, x.sy, x.sz, x.sc, sl.gidm, G.tab, tab_n, out, omega, err);
         }
         launched();
     });

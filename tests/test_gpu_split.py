@@ -2,7 +2,8 @@
 interior box plus the per-node code over the boundary shell) against the one-pass per-node sweep
 (AE_SPLIT=0, read when an operator is created).  Every node is computed with the per-node sweep's
 own arithmetic, so the results must be equal bit for bit (tolerance 0): FP32 Fsmooth on a single
-level of odd size (partial tiles, anisotropic spacing) and on refined patches with ghost layers
+level of 49 x 41 x 53 nodes (partial tiles, anisotropic spacing; the launch count shows the split
+ran) and on refined patches with ghost layers
 (inside the domain, and touching its low faces), m_uniform on and off, random BC tables, and
 whole mixed-precision solves.  Also: the padded row pitch of the level arrays (AE_PAD=0: dense)
 changes no result."""
@@ -11,13 +12,24 @@ import os
 import numpy as np
 import pytest
 
-from anisotropicfracture_gb300 import microstructure, models
+from anisotropicfracture_gb300 import _lib, microstructure, models
 from anisotropicfracture_gb300.elastic import Elastic, Field, Linear, level_desc
 from helpers import bc_random, polycrystal_amr
 from oracle import pyoracle as po
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
+
+
+def _single():
+    """One level of 49 x 41 x 53 nodes with anisotropic spacing: partial tiles in every direction.
+    Its cell counts are even, so it coarsens and keeps the padded row pitch the split sweep needs
+    (the coarsest level of AMR level 0 stays dense and runs the per-node kernels)."""
+    return po.level((48, 40, 52), dx=(1.0 / 48, 1.2 / 40, 0.9 / 52))
+
+
+def _launches():
+    return int(_lib.load().ae_kernel_launches())
 
 
 def _descs(Ls):
@@ -57,6 +69,16 @@ def _op(split, Ls, bc, gids, tab, uniform, pad=True):
     return op
 
 
+def _fsmooth_counted(op, a, L, x, b, sweeps, fs=None):
+    """_fsmooth (or fs), and the kernels it launched (after a call without sweeps, which makes
+    the FP32 copies)."""
+    fs = fs or _fsmooth
+    fs(op, a, L, x, b, 0)
+    n0 = _launches()
+    out = fs(op, a, L, x, b, sweeps)
+    return out, _launches() - n0
+
+
 def _fsmooth(op, a, L, x, b, sweeps):
     xd = torch.from_numpy(x.astype(np.float32)).cuda()
     bd = torch.from_numpy(b.astype(np.float32)).cuda()
@@ -67,15 +89,17 @@ def _fsmooth(op, a, L, x, b, sweeps):
 
 @pytest.mark.parametrize("uniform", [False, True])
 def test_split_sweep_equals_per_node_single_level(uniform):
-    Ls = [po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))]
+    Ls = [_single()]
     gids, tab = _grains(Ls)
     rng = np.random.default_rng(1)
     bc = bc_random(rng)
     x = rng.standard_normal((3,) + Ls[0].shape)
     b = rng.standard_normal((3,) + Ls[0].shape)
-    ref = _fsmooth(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3)
-    got = _fsmooth(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3)
+    ref, n_ref = _fsmooth_counted(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3)
+    got, n_split = _fsmooth_counted(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3)
     assert np.array_equal(got, ref), int((got != ref).sum())
+    # the split ran: two launches per sweep (tiled kernel and list) instead of one
+    assert n_split - n_ref == 3, (n_split, n_ref)
 
 
 @pytest.mark.parametrize("where", ["inside", "low_corner"])
@@ -131,14 +155,15 @@ def test_split_fp64_sweep_equals_per_node(uniform):
     """The FP64 split sweep (the reference's damped-Jacobi update, D read from its own tile)
     against the one-pass FP64 sweep, bit for bit: a single level and a refined patch."""
     rng = np.random.default_rng(7)
-    Ls = [po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))]
+    Ls = [_single()]
     gids, tab = _grains(Ls)
     bc = bc_random(rng)
     x = rng.standard_normal((3,) + Ls[0].shape)
     b = rng.standard_normal((3,) + Ls[0].shape)
-    ref = _fsmooth64(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3)
-    got = _fsmooth64(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3)
+    ref, n_ref = _fsmooth_counted(_op(False, Ls, bc, gids, tab, uniform, pad=False), 0, Ls[0], x, b, 3, _fsmooth64)
+    got, n_split = _fsmooth_counted(_op(True, Ls, bc, gids, tab, uniform), 0, Ls[0], x, b, 3, _fsmooth64)
     assert np.array_equal(got, ref), int((got != ref).sum())
+    assert n_split - n_ref == 3, (n_split, n_ref)
     Ls, _, bc, _ = polycrystal_amr(24, 2)
     gids, tab = _grains(Ls)
     for a, L in enumerate(Ls):
@@ -176,7 +201,7 @@ def test_split_fapply_equals_per_node(dtype):
     """Fapply through the split kernels (staged through the level's buffers) equals the one-pass
     per-node Fapply over the caller's fabs, bit for bit, on a single level and a refined patch."""
     rng = np.random.default_rng(12)
-    for Ls, bc in (([po.level((45, 38, 50), dx=(1.0 / 45, 1.2 / 38, 0.9 / 50))], bc_random(rng)),
+    for Ls, bc in (([_single()], bc_random(rng)),
                    (polycrystal_amr(24, 2)[0], bc_random(rng))):
         gids, tab = _grains(Ls)
         for a, L in enumerate(Ls):
@@ -209,3 +234,4 @@ def test_padded_pitch_changes_no_fp64_result():
     assert sols[0][0] == sols[1][0]
     for a, b in zip(sols[0][1], sols[1][1]):
         assert np.array_equal(a, b)
+
