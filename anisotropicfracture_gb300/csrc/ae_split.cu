@@ -40,7 +40,7 @@ namespace ae {
 namespace {
 
 constexpr int STX = 32, STY = 8, SNT = STX * STY;
-constexpr int SBW = 40;                    // box width: 32 nodes + halo + alignment shift
+constexpr int SBW = 36;                    // box width: 32 nodes + halo + alignment shift (<= 2)
 constexpr int SXR = STY + 2;               // x tile rows (one-node halo in j)
 constexpr int SXP = SBW * SXR;             // elements per x component plane tile
 constexpr int SVP = SBW * STY;             // elements per b / 1/D / D component tile (no halo)
@@ -49,8 +49,9 @@ constexpr int kWaitLimit = 1 << 20;        // try_wait polls before a wait is de
 #ifndef AE_SPLIT_MIN_BLOCKS
 #define AE_SPLIT_MIN_BLOCKS 4
 #endif
-// FP32: each thread computes the nodes of NPT consecutive rows (j, j + 1), which share the loads
-// of two rows of every plane: 28 instead of 38 shared-memory loads per component per pair
+// FP32: each thread computes the nodes of NPT consecutive rows j .. j + NPT - 1, which share the
+// loads of the rows between them in every plane: for two rows, 28 instead of 38 shared-memory
+// loads per component
 #ifndef AE_SPLIT_NPT32
 #define AE_SPLIT_NPT32 2
 #endif
@@ -193,19 +194,19 @@ struct TileGeo {
 // form in FP64, x + w (b - A x) / D in the FP32 cycle; Operator.cpp:109-157); OP = SPLIT_RESIDUAL,
 // out = b - A x (out may alias b: every node reads only its own b); OP = SPLIT_FAPPLY, out = A x.  The grain table is staged
 // in shared memory (TABS, rows padded to 16 bytes) or read through L1.  err: set when a TMA load
-// did not complete.  NPT: rows of the tile per thread (1, or 2: the thread's two nodes (i, j) and
-// (i, j + 1) take the x values of rows j - 1 .. j + 2 from one set of loads; each node's
+// did not complete.  NPT: rows of the tile per thread (1, 2 or 4: the thread's nodes (i, j) ..
+// (i, j + NPT - 1) take the x values of rows j - 1 .. j + NPT from one set of loads; each node's
 // arithmetic is unchanged).
 enum SplitOp { SPLIT_JACOBI = 0, SPLIT_RESIDUAL = 1, SPLIT_FAPPLY = 2 };
 template <int M, class R, bool TABS, int OP, int NPT>
-__global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
+__global__ void __launch_bounds__(SNT / NPT, NPT > 1 ? AE_SPLIT_PAIR_BLOCKS : sizeof(R) == 4 ? AE_SPLIT_MIN_BLOCKS : 2)
     k_sweep_tile(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_b,
                  const __grid_constant__ CUtensorMap tm_i, const __grid_constant__ CUtensorMap tm_d,
                  const __grid_constant__ CUtensorMap tm_g, SCoef<R> K, TileGeo T, int uniform, long long sy,
                  long long sz, long long sc, const unsigned* __restrict__ gidm_g, const R* __restrict__ tab, int tab_n,
                  R* __restrict__ xo, R omega, int* err) {
-    static_assert(NPT == 1 || NPT == 2, "one or two rows per thread");
-    static_assert(STY % NPT == 0, "whole row pairs per tile");
+    static_assert(NPT == 1 || NPT == 2 || NPT == 4, "one, two or four rows per thread");
+    static_assert(STY % NPT == 0, "whole row groups per tile");
     constexpr int NT = SNT / NPT;  // threads per block
     using L = TL<R>;
     constexpr int NC = NCoef<M>::value;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : s
     const int k1 = min(k0 + T.kz - 1, T.I.hi[2]);
     const int i = i0 + tx, j = j0 + ty;
     const bool act = i <= T.I.hi[0] && j <= T.I.hi[1];
-    const bool act1 = NPT == 2 && i <= T.I.hi[0] && j + 1 <= T.I.hi[1];  // the second node (implies act)
+    auto act_n = [&](int n) { return i <= T.I.hi[0] && j + n <= T.I.hi[1]; };  // node n of the thread
     // tensor coordinates of the boxes
     const int xa = i0 - 1 - T.slo[0] - T.sh;
     const int yx = j0 - 1 - T.slo[1], yv = j0 - T.slo[1];
@@ -357,29 +358,31 @@ __global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : s
                 queued[0] = !uniform && (gw >> 16) != 0;
             }
         } else {
-            queued[0] = queued[1] = false;
+#pragma unroll
+            for (int n = 0; n < NPT; ++n) queued[n] = false;
             if (act) {
-                // per component: plane k at rows j - 1 .. j + 2 and columns i - 1 .. i + 1 (12
-                // loads); planes k -+ 1 at rows j, j + 1 (three columns) and rows j - 1, j + 2
-                // (column i) (8 loads each).  Row r of these arrays is row j - 1 + r.
-                R h[2][3][6];
+                // per component: plane k at rows j - 1 .. j + NPT and columns i - 1 .. i + 1;
+                // planes k -+ 1 at rows j .. j + NPT - 1 (three columns) and rows j - 1, j + NPT
+                // (column i).  Row r of these arrays is row j - 1 + r.
+                constexpr int NR = NPT + 2;
+                R h[NPT][3][6];
 #pragma unroll
                 for (int p = 0; p < 3; ++p) {
                     const R* um = pm + p * SXP;
                     const R* uc = pc + p * SXP;
                     const R* up = pp + p * SXP;
-                    R ac[4][3], am[4][3], ap[4][3];
+                    R ac[NR][3], am[NR][3], ap[NR][3];
 #pragma unroll
-                    for (int r = 0; r < 4; ++r)
+                    for (int r = 0; r < NR; ++r)
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             ac[r][c] = uc[(r - 1) * SBW + c - 1];
-                            const bool need = (r == 1 || r == 2) || c == 1;
+                            const bool need = (r >= 1 && r <= NPT) || c == 1;
                             am[r][c] = need ? um[(r - 1) * SBW + c - 1] : R(0);
                             ap[r][c] = need ? up[(r - 1) * SBW + c - 1] : R(0);
                         }
 #pragma unroll
-                    for (int n = 0; n < 2; ++n) {
+                    for (int n = 0; n < NPT; ++n) {
                         const R c0 = ac[n + 1][1];
                         xv[n][p] = c0;
                         const R xm = ac[n + 1][0], xp = ac[n + 1][2], ym = ac[n][1], yp = ac[n + 2][1];
@@ -393,8 +396,8 @@ __global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : s
                     }
                 }
 #pragma unroll
-                for (int n = 0; n < 2; ++n) {
-                    if (n == 1 && !act1) break;
+                for (int n = 0; n < NPT; ++n) {
+                    if (n > 0 && !act_n(n)) break;
                     const unsigned gw = gring[vs * SVP + cv + n * SBW];
                     R bb[3][3][3];
 #pragma unroll
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(SNT / NPT, NPT == 2 ? AE_SPLIT_PAIR_BLOCKS : s
         // and row); the others are finished here
 #pragma unroll
         for (int n = 0; n < NPT; ++n) {
-            const bool an = n == 0 ? act : act1;
+            const bool an = n == 0 ? act : act && act_n(n);
             const unsigned ball = __ballot_sync(0xffffffffu, queued[n]);
             if (ball) {
                 const int lane = threadIdx.x & 31;
@@ -659,7 +662,11 @@ bool split_supported(const Geo& g) {
     const Box3 S = geo_store(g);
     for (int q = 0; q < 3; ++q)
         if (S.hi[q] - S.lo[q] >= (1 << 21)) return false;
-    return true;
+    // the tiles' column shift (TileGeo::sh) must leave the 34 columns of a tile inside the box:
+    // 0 on level 0 and on refined patches with 2 ghost layers, 1 or 2 where one touches the domain's
+    // low face
+    const Box3 I = split_interior(g);
+    return ((I.lo[0] - 1 - S.lo[0]) & 3) <= SBW - 34;
 }
 
 // count and fill the list of region R \ I (and, with gidm, the id/mask array)
