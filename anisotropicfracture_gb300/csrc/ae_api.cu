@@ -105,6 +105,9 @@ struct MGLevel {
     int* csr_col = nullptr;
     double* csr_val = nullptr;
     int csr_nnz = 0, csr_cap = 0;
+    int* csr_cptr = nullptr;  // chunks of the rows (BottomCsr)
+    int* csr_rch = nullptr;
+    int csr_nchunk = 0, csr_ccap = 0;
     bool csr_ok = false;
 };
 
@@ -393,8 +396,29 @@ void assemble_bottom(ae_op* op) {
         AE_CHECK(cudaMemcpyAsync(L.csr_col, cl.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
         AE_CHECK(cudaMemcpyAsync(L.csr_val, vl.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
     }
+    // chunks of at most kCsrChunk nonzeros, row by row (a row without nonzeros has one empty chunk)
+    std::vector<int> cp, rc((size_t)N + 1, 0);
+    for (long long r = 0; r < N; ++r) {
+        rc[(size_t)r] = (int)cp.size();
+        int q = rp[(size_t)r];
+        do {
+            cp.push_back(q);
+            q = std::min(q + kCsrChunk, rp[(size_t)r + 1]);
+        } while (q < rp[(size_t)r + 1]);
+    }
+    rc[(size_t)N] = (int)cp.size();
+    cp.push_back(nnz);
+    const int nchunk = (int)cp.size() - 1;
+    if (!L.csr_rch) L.csr_rch = op->alloc<int>(N + 1);
+    if (nchunk + 1 > L.csr_ccap) {
+        L.csr_cptr = op->alloc<int>(nchunk + 1);
+        L.csr_ccap = nchunk + 1;
+    }
+    AE_CHECK(cudaMemcpyAsync(L.csr_cptr, cp.data(), sizeof(int) * (nchunk + 1), cudaMemcpyHostToDevice, st));
+    AE_CHECK(cudaMemcpyAsync(L.csr_rch, rc.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, st));
     AE_CHECK(cudaStreamSynchronize(st));
     L.csr_nnz = nnz;
+    L.csr_nchunk = nchunk;
     L.csr_ok = true;
 }
 
@@ -624,7 +648,10 @@ struct Cycle {
         a.omega = o.omega;
         a.fail_count = op->dflag + 1;
         // the FP32 cycle's bottom: the same FP64 Krylov loop over the assembled level operator
-        if (sizeof(R) == 4 && L.csr_ok) launch_bottom_csr(a, BottomCsr{L.csr_rowptr, L.csr_col, L.csr_val, L.csr_nnz}, st);
+        if (sizeof(R) == 4 && L.csr_ok)
+            launch_bottom_csr(a, BottomCsr{L.csr_rowptr, L.csr_col, L.csr_val, L.csr_nnz, L.csr_cptr, L.csr_rch,
+                                           L.csr_nchunk},
+                              st);
         else launch_bottom(a, st);
         if (sizeof(R) == 4) launch_copy<R, double>(s, 3, level_view(L.g, ptrs<R>(L).cor), cview(level_view(L.g, L.cor)), st);
     }

@@ -731,18 +731,38 @@ void launch_bottom_assemble(const BottomArgs& a, double* A, double* E, cudaStrea
     launched();
 }
 
-// Krylov operations over the CSR rows (one thread per row, fixed order: deterministic)
+// Krylov operations over the CSR rows (fixed order: deterministic).  With chunks (part != null)
+// a thread sums the products of a chunk into part[], then a thread per row adds its chunks in
+// order; else one thread per row.
 struct CsrOps {
     const BottomArgs& a;
     const int* rowptr;
     const int* col;
     const double* val;
     int N;
+    const int* cptr = nullptr;
+    const int* rch = nullptr;
+    double* part = nullptr;
+    int nchunk = 0;
     __device__ void apply(const double* x, double* out, BlkRed&) const {
-        for (int r = threadIdx.x; r < N; r += blockDim.x) {
-            double s = 0.0;
-            for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) s += val[q] * x[col[q]];
-            out[r] = s;
+        if (part) {
+            for (int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+                double s = 0.0;
+                for (int q = cptr[c]; q < cptr[c + 1]; ++q) s += val[q] * x[col[q]];
+                part[c] = s;
+            }
+            __syncthreads();
+            for (int r = threadIdx.x; r < N; r += blockDim.x) {
+                double s = part[rch[r]];
+                for (int c = rch[r] + 1; c < rch[r + 1]; ++c) s += part[c];
+                out[r] = s;
+            }
+        } else {
+            for (int r = threadIdx.x; r < N; r += blockDim.x) {
+                double s = 0.0;
+                for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) s += val[q] * x[col[q]];
+                out[r] = s;
+            }
         }
         __syncthreads();
     }
@@ -792,13 +812,28 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, Bot
         double* sb = sval + m.nnz;
         double* sx = sb + N;
         double* sw = sx + N;
-        int* srow = reinterpret_cast<int*>(sw + 8 * N);
+        double* spart = sw + 8 * N;
+        int* srow = reinterpret_cast<int*>(spart + (m.cptr ? m.nchunk : 0));
         int* scol = srow + N + 1;
+        int* scp = scol + m.nnz;
+        int* src = scp + m.nchunk + 1;
         for (long long t = threadIdx.x; t < m.nnz; t += blockDim.x) { sval[t] = m.val[t]; scol[t] = m.col[t]; }
         for (long long t = threadIdx.x; t <= N; t += blockDim.x) srow[t] = m.rowptr[t];
         for (int t = threadIdx.x; t < N; t += blockDim.x) { sb[t] = a.b[t]; sx[t] = a.x[t]; }
+        if (m.cptr) {
+            for (int t = threadIdx.x; t <= m.nchunk; t += blockDim.x) scp[t] = m.cptr[t];
+            for (int t = threadIdx.x; t <= N; t += blockDim.x) src[t] = m.rch[t];
+        }
         __syncthreads();
         rowptr = srow; col = scol; val = sval; b = sb; x = sx; work = sw;
+        if (m.cptr) {
+            const CsrOps ops{a, rowptr, col, val, N, scp, src, spart, m.nchunk};
+            const KrylovParams kp{a.bottom, a.maxiter, a.reltol, a.nuf};
+            const int ret = krylov_bottom(ops, kp, N, x, b, work, sh);
+            if (ret != 0 && ret != 9 && threadIdx.x == 0 && a.fail_count) atomicAdd(a.fail_count, 1);
+            for (int t = threadIdx.x; t < N; t += blockDim.x) a.x[t] = x[t];
+            return;
+        }
     }
     const CsrOps ops{a, rowptr, col, val, N};
     const KrylovParams kp{a.bottom, a.maxiter, a.reltol, a.nuf};
@@ -809,15 +844,15 @@ __global__ void __launch_bounds__(kBottomThreads) k_bottom_csr(BottomArgs a, Bot
     }
 }
 
-size_t bottom_csr_smem_bytes(long long N, long long nnz) {
-    return (size_t)(nnz + 10 * N) * sizeof(double) + (size_t)(N + 1 + nnz) * sizeof(int);
+size_t bottom_csr_smem_bytes(long long N, long long nnz, long long nchunk) {
+    return (size_t)(nnz + 10 * N + nchunk) * sizeof(double) + (size_t)(N + 1 + nnz + nchunk + 1 + N + 1) * sizeof(int);
 }
 
-// one thread per row, rounded up to whole warps
+// one thread per row or chunk, rounded up to whole warps
 void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st) {
     const int N = (int)(3 * a.nn);
-    const int threads = (int)std::min<long long>(kBottomThreads, (N + 31) / 32 * 32);
-    const size_t bytes = bottom_csr_smem_bytes(N, m.nnz);
+    const int threads = (int)std::min<long long>(kBottomThreads, (std::max(N, m.nchunk) + 31) / 32 * 32);
+    const size_t bytes = bottom_csr_smem_bytes(N, m.nnz, m.cptr ? m.nchunk : 0);
     if (bytes <= kBottomSmemBytes) k_bottom_csr<true><<<1, threads, bytes, st>>>(a, m);
     else k_bottom_csr<false><<<1, threads, 0, st>>>(a, m);
     launched();

@@ -225,7 +225,15 @@ struct BottomCsr {
     const int* col;
     const double* val;
     int nnz;
+    // the nonzeros cut into chunks of at most kCsrChunk consecutive entries of one row: chunk c is
+    // [cptr[c], cptr[c + 1]), the chunks of row r are [rch[r], rch[r + 1]) (null: none)
+    const int* cptr = nullptr;
+    const int* rch = nullptr;
+    int nchunk = 0;
 };
+// nonzeros per chunk of the bottom's sparse product: one thread sums a chunk, then each row adds
+// its chunks' sums, so a long row's dependent FP64 chain is a few chunks long, not the whole row
+constexpr int kCsrChunk = 8;
 void launch_bottom_assemble(const BottomArgs& a, double* A, double* E, cudaStream_t st);
 void launch_bottom_csr(const BottomArgs& a, const BottomCsr& m, cudaStream_t st);
 // unknowns up to which the coarsest level is assembled (dense scratch 2 N^2 doubles at set-up)
