@@ -703,13 +703,15 @@ inline unsigned flat_blocks(long long n) {
     return (unsigned)(b < 152 * 8 ? b : 152 * 8);
 }
 
+// max-norm of a region: grid-stride over the nodes with a capped grid (kNormBlocks), so that a
+// few thousand blocks, not one per 256 nodes, end in a barrier and an atomic
+constexpr unsigned kNormBlocks = 152 * 8;
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_norminf(Reg reg, int ncomp, View<const R> v, unsigned long long* out) {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     double mx = 0.0;
-    if (t < reg.n) {
+    for (unsigned long long t = blockIdx.x * blockDim.x + threadIdx.x; t < reg.n; t += gridDim.x * blockDim.x) {
         int i, j, k;
-        reg_ijk(reg, t, i, j, k);
+        reg_ijk(reg, (unsigned)t, i, j, k);
         const long long o = v.at(i, j, k);
         for (int n = 0; n < ncomp; ++n) {
             const R a = v.p[o + n * v.sc];
