@@ -1,4 +1,4 @@
-// Split FP32 sweeps on Voronoi (grain-map) levels.
+// Split sweeps on Voronoi (grain-map) levels, FP32 and FP64.
 //
 // On a grain-map level the per-node sweep spends most of its issue slots on work that few nodes
 // need -- the domain-boundary classification, six neighbour grain ids, the grad C branch that
@@ -11,20 +11,22 @@
 //                  mbarrier, the x halo tile (three components), b, 1/D and the grain id/mask
 //                  tile of the next plane, so every read of the stencil and the update is a
 //                  shared-memory load at a fixed offset.  The grain table sits in shared memory.
-//                  The grad C term is computed only where the node's mask says a direction's two
-//                  neighbours lie in different grains.
+//                  In FP32 a thread computes the nodes of two neighbouring rows, which share the
+//                  loads of the rows between them.  The grad C term is computed only where the
+//                  node's mask says a direction's two neighbours lie in different grains.
 //   k_*_list       every node of the sweep region outside I (domain-boundary rows, the ghost
 //                  ring, nodes outside the domain), through the per-node code.
 //
-// Two sweeps are split this way: the damped-Jacobi smoother and the correction residual
-// r = b - A x of the FP32 cycle.
+// Three operations are split this way: the damped-Jacobi smoother, the residual r = b - A x and
+// Fapply.
 //
 // Every node is computed by the per-node sweep's own arithmetic: where a direction's neighbours
 // share a grain the grad C column is exactly zero, and the interior and grad C expressions are
-// written operation for operation as apply_node_grains writes them, so the split sweep equals the
-// one-pass sweep bit for bit.  The list and the id/mask array are built once per level
-// (k_split_mark), when the FP32 copies are made.  TMA needs 16-byte aligned rows: the level
-// arrays' row pitch is a multiple of 4 nodes (Geo::px).
+// written operation for operation as apply_node_grains writes them (the FP32 sums of products in
+// the explicitly rounded order of ae_device.cuh), so the split sweep equals the one-pass sweep
+// bit for bit.  The list and the id/mask array are built once per level (k_split_mark), when the
+// operator is prepared.  TMA needs 16-byte aligned rows: the level arrays' row pitch is a
+// multiple of 4 nodes (Geo::px).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
