@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/aefast.h"
+#include "ae_csr_chunks.h"
 #include "ae_launch.h"
 #include "ae_split.h"
 
@@ -396,18 +397,9 @@ void assemble_bottom(ae_op* op) {
         AE_CHECK(cudaMemcpyAsync(L.csr_col, cl.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
         AE_CHECK(cudaMemcpyAsync(L.csr_val, vl.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
     }
-    // chunks of at most kCsrChunk nonzeros, row by row (a row without nonzeros has one empty chunk)
-    std::vector<int> cp, rc((size_t)N + 1, 0);
-    for (long long r = 0; r < N; ++r) {
-        rc[(size_t)r] = (int)cp.size();
-        int q = rp[(size_t)r];
-        do {
-            cp.push_back(q);
-            q = std::min(q + kCsrChunk, rp[(size_t)r + 1]);
-        } while (q < rp[(size_t)r + 1]);
-    }
-    rc[(size_t)N] = (int)cp.size();
-    cp.push_back(nnz);
+    // chunks of at most kCsrChunk nonzeros, row by row
+    std::vector<int> cp, rc;
+    csr_chunks(rp, kCsrChunk, cp, rc);
     const int nchunk = (int)cp.size() - 1;
     if (!L.csr_rch) L.csr_rch = op->alloc<int>(N + 1);
     if (nchunk + 1 > L.csr_ccap) {
